@@ -1,0 +1,360 @@
+"""ctypes wrapper of the CPU oracle (fqsb_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and by
+bench.py's CPU-baseline / reference arm, always as the checker.  The product
+package never imports this module.
+
+The wrapper classes mirror the reference's Python API
+(python/main.cpp:46-226 in the reference project) so that oracle-backed tests
+read like the reference's own tests.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import pathlib
+import subprocess
+
+import numpy as np
+
+HERE = pathlib.Path(__file__).resolve().parent
+BUILD = HERE / "_build"
+LIB = BUILD / "libfqsb_oracle.so"
+SOURCES = [HERE / "fqsb_oracle.c", HERE / "fqsb_oracle.h", HERE.parent / "frictionqpotspringblock_gb300" / "csrc" / "fq_math.h"]
+
+CUSPY, SEMISMOOTH, SMOOTH = 0, 1, 2
+NONE, LAPLACE1D, LAPLACE2D = 0, 1, 2
+SUM_SEQUENTIAL, SUM_PAIRWISE = 0, 1
+MATH_LIBM, MATH_PORTABLE = 0, 1
+DISTRIBUTIONS = {
+    "random": 0,
+    "delta": 1,
+    "exponential": 2,
+    "power": 3,
+    "gamma": 4,
+    "pareto": 5,
+    "weibull": 6,
+    "normal": 7,
+}
+F_U, F_V, F_A, F_F, F_POT, F_INT, F_FRAME, F_DAMP = range(8)
+S_U_FRAME, S_T, S_TEMPERATURE, S_RESIDUAL, S_MEAN_F_FRAME = range(5)
+
+
+def build(force: bool = False) -> pathlib.Path:
+    """Compile the oracle with gcc (no FMA contraction, no fast-math)."""
+    BUILD.mkdir(exist_ok=True)
+    newest = max(p.stat().st_mtime for p in SOURCES)
+    if force or not LIB.exists() or LIB.stat().st_mtime < newest:
+        tmp = BUILD / f"libfqsb_oracle.{os.getpid()}.so"
+        cmd = [
+            "gcc", "-std=gnu11", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
+            "-o", str(tmp), str(HERE / "fqsb_oracle.c"), "-lm",
+        ]
+        subprocess.run(cmd, check=True)
+        os.replace(tmp, LIB)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(str(LIB))
+        P = ctypes.c_void_p
+        d, i64, u64, i32 = ctypes.c_double, ctypes.c_int64, ctypes.c_uint64, ctypes.c_int
+        pd = ctypes.POINTER(ctypes.c_double)
+        L.oq_create.restype = P
+        L.oq_create.argtypes = [i32, i32, i64, i64, d, d, d, d, d, d, d, u64, i32, pd, i32, d, pd, i64, i32, i32]
+        L.oq_destroy.argtypes = [P]
+        L.oq_last_error.restype = ctypes.c_char_p
+        L.oq_last_error.argtypes = [P]
+        L.oq_size.restype = i64
+        L.oq_size.argtypes = [P]
+        L.oq_pcg32_stream.restype = ctypes.c_uint32
+        L.oq_pcg32_stream.argtypes = [u64, u64, i64, P]
+        L.oq_pcg32_advance.restype = u64
+        L.oq_pcg32_advance.argtypes = [u64, u64, i64]
+        L.oq_transform.restype = d
+        L.oq_transform.argtypes = [i32, pd, i32, ctypes.c_uint32, i32]
+        L.oq_math.restype = d
+        L.oq_math.argtypes = [i32, d, d, i32]
+        L.oq_get.argtypes = [P, i32, P]
+        L.oq_set.argtypes = [P, i32, P]
+        L.oq_get_scalar.restype = d
+        L.oq_get_scalar.argtypes = [P, i32]
+        L.oq_set_u_frame.argtypes = [P, d]
+        L.oq_set_inc.argtypes = [P, i64]
+        L.oq_get_inc.restype = i64
+        L.oq_get_inc.argtypes = [P]
+        L.oq_set_t.argtypes = [P, d]
+        L.oq_get_index.argtypes = [P, P, P, P, P]
+        L.oq_chunk_data.argtypes = [P, P, P]
+        L.oq_chunk_state_at.argtypes = [P, P, P]
+        L.oq_chunk_restore.argtypes = [P, P, P, P]
+        L.oq_yield_sequence.argtypes = [P, i64, i64, i64, P]
+        L.oq_quasistatic_first.restype = i64
+        L.oq_quasistatic_first.argtypes = [P]
+        L.oq_quasistatic_last.restype = i64
+        L.oq_quasistatic_last.argtypes = [P]
+        for name in ("oq_refresh", "oq_quench", "oq_time_step"):
+            getattr(L, name).argtypes = [P]
+        L.oq_time_steps.argtypes = [P, u64]
+        L.oq_flow_steps.argtypes = [P, u64, d]
+        L.oq_time_steps_until_event.argtypes = [P, d, u64, u64, ctypes.POINTER(u64)]
+        L.oq_minimise.argtypes = [P, d, u64, u64, i32, i32, ctypes.POINTER(u64)]
+        L.oq_minimise_truncate.argtypes = [P, P, u64, u64, d, u64, u64, i32, i32, ctypes.POINTER(u64)]
+        L.oq_max_uniform_displacement.argtypes = [P, i32, pd]
+        L.oq_event_driven_step.argtypes = [P, d, i32, i32, pd]
+        L.oq_trigger.argtypes = [P, i64, d, i32]
+        L.oq_advance_to_fixed_force.argtypes = [P, d, i32]
+        _lib = L
+    return _lib
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def pcg32_stream(initstate: int, initseq: int, n: int) -> np.ndarray:
+    out = np.empty(n, dtype=np.uint32)
+    lib().oq_pcg32_stream(initstate, initseq, n, _ptr(out))
+    return out
+
+
+def pcg32_advance(state: int, inc: int, delta: int) -> int:
+    return int(lib().oq_pcg32_advance(state, inc, delta))
+
+
+def transform(distribution: str, parameters, r32: int, math_mode: int = MATH_PORTABLE) -> float:
+    par = (ctypes.c_double * 4)(*list(parameters))
+    return lib().oq_transform(DISTRIBUTIONS[distribution], par, len(parameters), r32, math_mode)
+
+
+def math(which: str, x: float, y: float = 0.0, math_mode: int = MATH_PORTABLE) -> float:
+    return lib().oq_math({"log": 0, "pow": 1, "sin": 2, "exp": 3}[which], x, y, math_mode)
+
+
+class OracleError(RuntimeError):
+    pass
+
+
+class _Chunk:
+    """The prrng chunk members the reference's tests use (test_Line1d.py:83-86, 309-326)."""
+
+    def __init__(self, sys):
+        self._s = sys
+
+    def _idx(self):
+        s = self._s
+        g = np.empty(s.size, np.int64)
+        c = np.empty(s.size, np.int64)
+        left = np.empty(s.size)
+        right = np.empty(s.size)
+        lib().oq_get_index(s._h, _ptr(g), _ptr(c), _ptr(left), _ptr(right))
+        shape = s.shape
+        return g.reshape(shape), c.reshape(shape), left.reshape(shape), right.reshape(shape)
+
+    @property
+    def index_at_align(self):
+        return self._idx()[0]
+
+    @property
+    def chunk_index_at_align(self):
+        return self._idx()[1]
+
+    @property
+    def left_of_align(self):
+        return self._idx()[2]
+
+    @property
+    def right_of_align(self):
+        return self._idx()[3]
+
+    @property
+    def data(self):
+        s = self._s
+        out = np.empty((s.size, s.nchunk))
+        lib().oq_chunk_data(s._h, _ptr(out), None)
+        return out.reshape(tuple(s.shape) + (s.nchunk,))
+
+    @property
+    def start(self):
+        s = self._s
+        out = np.empty(s.size, np.int64)
+        lib().oq_chunk_data(s._h, None, _ptr(out))
+        return out.reshape(s.shape)
+
+    def state_at(self, index):
+        s = self._s
+        idx = np.ascontiguousarray(np.broadcast_to(index, s.shape), dtype=np.int64).ravel()
+        out = np.empty(s.size, np.uint64)
+        lib().oq_chunk_state_at(s._h, _ptr(idx), _ptr(out))
+        return out.reshape(s.shape)
+
+    def restore(self, state, value, index):
+        s = self._s
+        st = np.ascontiguousarray(state, dtype=np.uint64).ravel()
+        val = np.ascontiguousarray(value, dtype=np.float64).ravel()
+        idx = np.ascontiguousarray(index, dtype=np.int64).ravel()
+        lib().oq_chunk_restore(s._h, _ptr(st), _ptr(val), _ptr(idx))
+
+
+class System:
+    """Oracle system with the reference's attribute and method names."""
+
+    def __init__(self, potential, interactions, shape, m, eta, mu, k_interactions, k_frame, dt, seed,
+                 distribution, parameters, offset=-100.0, nchunk=5000, kappa=0.0, offset_per_particle=None,
+                 sum_mode=SUM_PAIRWISE, math_mode=MATH_PORTABLE):
+        shape = [int(i) for i in shape]
+        rows, cols = (1, shape[0]) if len(shape) == 1 else (shape[0], shape[1])
+        self.shape = shape
+        self.size = rows * cols
+        self.nchunk = int(nchunk)
+        par = (ctypes.c_double * 4)(*list(parameters))
+        offp = None
+        if offset_per_particle is not None:
+            self._offp = np.ascontiguousarray(offset_per_particle, dtype=np.float64).ravel()
+            offp = self._offp.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        h = lib().oq_create(potential, interactions, rows, cols, m, eta, mu, kappa, k_interactions, k_frame, dt,
+                            int(seed), DISTRIBUTIONS[distribution], par, len(parameters), offset, offp, nchunk,
+                            sum_mode, math_mode)
+        if not h:
+            raise OracleError("invalid oracle configuration")
+        self._h = h
+        self.dt, self.mu, self.eta, self.m, self.k_frame = dt, mu, eta, m, k_frame
+        self.chunk = _Chunk(self)
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().oq_destroy(self._h)
+            self._h = None
+
+    def _check(self, rc):
+        if rc != 0:
+            raise OracleError(lib().oq_last_error(self._h).decode())
+
+    def _get(self, field):
+        out = np.empty(self.size)
+        lib().oq_get(self._h, field, _ptr(out))
+        return out.reshape(self.shape)
+
+    def _set(self, field, value):
+        arr = np.ascontiguousarray(np.broadcast_to(value, self.shape), dtype=np.float64)
+        self._check(lib().oq_set(self._h, field, _ptr(arr)))
+
+    u = property(lambda s: s._get(F_U), lambda s, x: s._set(F_U, x))
+    v = property(lambda s: s._get(F_V), lambda s, x: s._set(F_V, x))
+    a = property(lambda s: s._get(F_A), lambda s, x: s._set(F_A, x))
+    f = property(lambda s: s._get(F_F))
+    f_potential = property(lambda s: s._get(F_POT))
+    f_interactions = property(lambda s: s._get(F_INT))
+    f_frame = property(lambda s: s._get(F_FRAME))
+    f_damping = property(lambda s: s._get(F_DAMP))
+    temperature = property(lambda s: lib().oq_get_scalar(s._h, S_TEMPERATURE))
+    residual = property(lambda s: lib().oq_get_scalar(s._h, S_RESIDUAL))
+    mean_f_frame = property(lambda s: lib().oq_get_scalar(s._h, S_MEAN_F_FRAME))
+    quasistaticActivityFirst = property(lambda s: lib().oq_quasistatic_first(s._h))
+    quasistaticActivityLast = property(lambda s: lib().oq_quasistatic_last(s._h))
+
+    @property
+    def u_frame(self):
+        return lib().oq_get_scalar(self._h, S_U_FRAME)
+
+    @u_frame.setter
+    def u_frame(self, value):
+        lib().oq_set_u_frame(self._h, float(value))
+
+    @property
+    def inc(self):
+        return lib().oq_get_inc(self._h)
+
+    @inc.setter
+    def inc(self, value):
+        lib().oq_set_inc(self._h, int(value))
+
+    @property
+    def t(self):
+        return lib().oq_get_scalar(self._h, S_T)
+
+    @t.setter
+    def t(self, value):
+        lib().oq_set_t(self._h, float(value))
+
+    @property
+    def i(self):
+        return self.chunk.index_at_align
+
+    def refresh(self):
+        lib().oq_refresh(self._h)
+
+    def quench(self):
+        lib().oq_quench(self._h)
+
+    def timeStep(self):
+        self._check(lib().oq_time_step(self._h))
+
+    def timeSteps(self, n):
+        self._check(lib().oq_time_steps(self._h, int(n)))
+
+    def flowSteps(self, n, v_frame):
+        self._check(lib().oq_flow_steps(self._h, int(n), float(v_frame)))
+
+    def timeStepsUntilEvent(self, tol=1e-5, niter_tol=10, max_iter=int(1e9)):
+        r = ctypes.c_uint64()
+        self._check(lib().oq_time_steps_until_event(self._h, tol, niter_tol, max_iter, ctypes.byref(r)))
+        return r.value
+
+    def minimise(self, tol=1e-5, niter_tol=10, max_iter=int(1e9), time_activity=False, max_iter_is_error=True):
+        r = ctypes.c_uint64()
+        self._check(lib().oq_minimise(self._h, tol, niter_tol, int(max_iter), int(time_activity),
+                                      int(max_iter_is_error), ctypes.byref(r)))
+        return r.value
+
+    def minimise_truncate(self, i_n, A_truncate=0, S_truncate=0, tol=1e-5, niter_tol=10, max_iter=int(1e9),
+                          time_activity=True, max_iter_is_error=True):
+        idx = np.ascontiguousarray(i_n, dtype=np.int64).ravel()
+        r = ctypes.c_uint64()
+        self._check(lib().oq_minimise_truncate(self._h, _ptr(idx), A_truncate, S_truncate, tol, niter_tol,
+                                               int(max_iter), int(time_activity), int(max_iter_is_error),
+                                               ctypes.byref(r)))
+        return r.value
+
+    def maxUniformDisplacement(self, direction=1):
+        r = ctypes.c_double()
+        self._check(lib().oq_max_uniform_displacement(self._h, direction, ctypes.byref(r)))
+        return r.value
+
+    def eventDrivenStep(self, eps, kick, direction=1):
+        r = ctypes.c_double()
+        self._check(lib().oq_event_driven_step(self._h, eps, int(kick), direction, ctypes.byref(r)))
+        return r.value
+
+    def trigger(self, p, eps, direction=1):
+        self._check(lib().oq_trigger(self._h, int(p), eps, direction))
+
+    def advanceToFixedForce(self, f_frame, allow_plastic=False):
+        self._check(lib().oq_advance_to_fixed_force(self._h, f_frame, int(allow_plastic)))
+
+    def yield_sequence(self, p, k0, count):
+        out = np.empty(count)
+        self._check(lib().oq_yield_sequence(self._h, p, k0, count, _ptr(out)))
+        return out
+
+
+def line1d(potential="Cuspy", **kw):
+    pot = {"Cuspy": CUSPY, "SemiSmooth": SEMISMOOTH, "Smooth": SMOOTH}[potential]
+    return System(pot, LAPLACE1D, **kw)
+
+
+def line2d(**kw):
+    return System(CUSPY, LAPLACE2D, **kw)
+
+
+def particles(potential="Cuspy", **kw):
+    pot = {"Cuspy": CUSPY, "SemiSmooth": SEMISMOOTH, "Smooth": SMOOTH}[potential]
+    kw.setdefault("k_interactions", 0.0)
+    return System(pot, NONE, **kw)
