@@ -1,0 +1,611 @@
+/*
+ * Device-side building blocks of the time-integration path (sm_103a, FP64).
+ *
+ * All floating-point arithmetic goes through __dadd_rn / __dmul_rn / ...
+ * (FQ_* macros), so nvcc cannot contract it into fma and every kernel
+ * reproduces the reference's operation order exactly
+ * (include/FrictionQPotSpringBlock/detail.h:1539-1570 and the force functions
+ * it calls).
+ *
+ * Disorder ("chunk"): per particle a window of W yield positions of the
+ * particle's canonical yield sequence, plus the particle's current well
+ * (yl, yr) and derived constants cached in one double4.  The canonical
+ * sequence (one definition, independent of where the window sits):
+ *     0 <= k < n0 : c_0 = d_0, c_k = c_{k-1} + d_k, y_k = c_k + offset
+ *     k >= n0     : y_k = y_{k-1} + d_k
+ *     k < 0       : y_k = y_{k+1} - d_{k+1}
+ * with d_k the distribution transform of the k-th pcg32 output of the
+ * particle's generator (initstate = seed + p, initseq = 0) and n0 = nchunk;
+ * after chunk.restore(state, value, index) the sequence is redefined relative
+ * to that anchor (y_index = value, forward by addition, backward by
+ * subtraction).  This restates prrng's pcg32_tensor_cumsum (the reference's
+ * Generator, Line1d.h:51-52) as used by the reference.
+ */
+#ifndef FQSB_DEVICE_CUH
+#define FQSB_DEVICE_CUH
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fq_math.h"
+
+namespace fqsb {
+
+constexpr uint64_t PCG_MULT = 0x5851f42d4c957f2dULL;
+
+enum : int { POT_CUSPY = 0, POT_SEMISMOOTH = 1, POT_SMOOTH = 2 };
+enum : int { INTER_NONE = 0, INTER_LAPLACE1D = 1, INTER_LAPLACE2D = 2 };
+enum : int {
+    DIST_RANDOM = 0,
+    DIST_DELTA = 1,
+    DIST_EXPONENTIAL = 2,
+    DIST_POWER = 3,
+    DIST_GAMMA = 4,
+    DIST_PARETO = 5,
+    DIST_WEIBULL = 6,
+    DIST_NORMAL = 7
+};
+
+/* termination codes of a stepping run (Ctl::done) */
+enum : int { RUN_ACTIVE = 0, RUN_CONVERGED = 1, RUN_MAXITER = 2, RUN_EVENT = 3, RUN_TRUNCATED = 4 };
+/* error codes (Ctl::error), equal to fqsb_status */
+enum : int { DERR_NONE = 0, DERR_NAN = 1, DERR_WALK = 5 };
+
+/* Upper bound on the draws one yield search may walk through; beyond it the search gives up
+ * (flagging Ctl::walk_flag) instead of running for an unbounded time. */
+constexpr int64_t MAX_WALK = int64_t(1) << 26;
+/* run flags (Ctl::flags) */
+enum : int { RF_RESID = 1, RF_ACT = 2, RF_FLOW = 4, RF_EVENT = 8, RF_TRUNCATE = 16 };
+
+/* Control block of a stepping run; lives in device memory, written by the host before a run and
+ * by the last CTA of every step. */
+struct Ctl {
+    /* run parameters */
+    int64_t max_steps;
+    double tol, tol2;
+    int64_t niter_tol;
+    int32_t flags;
+    int32_t pad0;
+    double vdt; /* v_frame * dt for flowSteps */
+    int64_t A_truncate, S_truncate;
+    /* run state */
+    int32_t cur;
+    int32_t done;
+    int32_t error;
+    uint32_t ticket;
+    int64_t step;
+    int64_t inc;
+    double u_frame;
+    /* StopList (GooseFEM::Iterate::StopList): ring + counters */
+    int64_t sl_pos, sl_ge_tol, sl_ge_tol2, sl_asc;
+    /* activity (detail.h:1768-1778, 1855-1866) */
+    int64_t s_sum, a_count, s_n;
+    int32_t init;
+    int32_t nan_flag;
+    int32_t walk_flag; /* a yield search exceeded MAX_WALK (absurd target): reported as an error */
+    int32_t pad1;
+    int64_t qs_first, qs_last;
+    /* last residual (for diagnostics) */
+    double last_residual;
+};
+
+struct DevSys {
+    int64_t N, rows, cols;
+    int pot, inter;
+    double dt, hdt, hdt2, mu, kappa, k, k_frame, me, inv_m, m;
+    /* chunk */
+    int64_t W, n0;
+    int dist, npar;
+    double par[4];
+    double offset;
+    const double* offp;
+    uint64_t seed;
+    int64_t buffer, margin, min_margin;
+    double* data;
+    int64_t* start;
+    int32_t* cidx;
+    int64_t* gidx;
+    double4_32a* wc;
+    double* acc_end;
+    uint8_t* anc_kind;
+    int64_t* anc_k;
+    uint64_t* anc_state;
+    double* anc_val;
+    /* state, double buffered */
+    double* u[2];
+    double* v[2];
+    double* a[2];
+    /* run control */
+    Ctl* ctl;
+    double* ring;
+    double2* partials;
+    int64_t* i_n;
+    double2* sq2;
+    int64_t npartials;
+};
+
+/* ------------------------------------------------------------ pcg32 */
+
+__device__ __forceinline__ uint32_t pcg_output(uint64_t old)
+{
+    uint32_t xs = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+    uint32_t rot = (uint32_t)(old >> 59u);
+    return __funnelshift_r(xs, xs, rot);
+}
+
+__device__ __forceinline__ uint64_t pcg_step(uint64_t s)
+{
+    return s * PCG_MULT + 1ULL; /* initseq = 0 => inc = 1 */
+}
+
+/* pcg32_srandom_r(initstate, initseq = 0) */
+__device__ __forceinline__ uint64_t pcg_seed(uint64_t initstate)
+{
+    uint64_t s = pcg_step(0ULL);
+    s += initstate;
+    return pcg_step(s);
+}
+
+/* LCG jump-ahead by delta (mod 2^64), Brown (1994) */
+static __device__ __noinline__ uint64_t pcg_advance(uint64_t state, uint64_t delta)
+{
+    uint64_t cur_mult = PCG_MULT, cur_plus = 1ULL, acc_mult = 1ULL, acc_plus = 0ULL;
+    while (delta > 0) {
+        if (delta & 1ULL) {
+            acc_mult *= cur_mult;
+            acc_plus = acc_plus * cur_mult + cur_plus;
+        }
+        cur_plus = (cur_mult + 1ULL) * cur_plus;
+        cur_mult *= cur_mult;
+        delta >>= 1u;
+    }
+    return acc_mult * state + acc_plus;
+}
+
+__device__ __forceinline__ double par_or(const DevSys& s, int i, double def)
+{
+    return i < s.npar ? s.par[i] : def;
+}
+
+/* prrng distribution transform of one draw; same expressions and order as the oracle */
+static __device__ __noinline__ double dev_transform(const DevSys& s, uint32_t r32)
+{
+    double r = FQ_MUL((double)r32, 0x1p-32);
+    switch (s.dist) {
+        case DIST_RANDOM:
+            return FQ_ADD(FQ_MUL(r, par_or(s, 0, 1.0)), par_or(s, 1, 0.0));
+        case DIST_DELTA:
+            return FQ_ADD(par_or(s, 0, 1.0), par_or(s, 1, 0.0));
+        case DIST_EXPONENTIAL:
+            return FQ_ADD(FQ_MUL(-fq_log(FQ_SUB(1.0, r)), par_or(s, 0, 1.0)), par_or(s, 1, 0.0));
+        case DIST_POWER:
+            return FQ_ADD(fq_pow(r, FQ_DIV(1.0, par_or(s, 0, 1.0))), par_or(s, 1, 0.0));
+        case DIST_PARETO:
+            return FQ_ADD(FQ_DIV(par_or(s, 1, 1.0), fq_pow(FQ_SUB(1.0, r), FQ_DIV(1.0, par_or(s, 0, 1.0)))),
+                          par_or(s, 2, 0.0));
+        case DIST_WEIBULL:
+            return FQ_ADD(FQ_MUL(par_or(s, 1, 1.0), fq_pow(-fq_log(FQ_SUB(1.0, r)), FQ_DIV(1.0, par_or(s, 0, 1.0)))),
+                          par_or(s, 2, 0.0));
+        default:
+            return __longlong_as_double(0x7ff8000000000000LL);
+    }
+}
+
+__device__ __forceinline__ double dev_draw(const DevSys& s, uint64_t st)
+{
+    return dev_transform(s, s.dist == DIST_DELTA ? 0u : pcg_output(st));
+}
+
+__device__ __forceinline__ double off_of(const DevSys& s, int64_t p)
+{
+    return s.offp ? s.offp[p] : s.offset;
+}
+
+/* origin of the particle's sequence: index, and pcg32 state whose output is d_origin */
+__device__ __forceinline__ void seq_origin(const DevSys& s, int64_t p, int& kind, int64_t& k0, uint64_t& st0)
+{
+    kind = s.anc_kind[p];
+    if (kind) {
+        k0 = s.anc_k[p];
+        st0 = s.anc_state[p];
+    }
+    else {
+        k0 = 0;
+        st0 = pcg_seed(s.seed + (uint64_t)p);
+    }
+}
+
+/*
+ * Canonical y_k for k in [k0, k0+cnt) written to out[0..cnt), replayed from the particle's origin.
+ * Also returns, if acc_last != NULL, the running accumulator at index k0+cnt-1 (c_k inside the
+ * initial region 0 <= k < n0, else y_k), which lets a later forward extension continue exactly.
+ */
+static __device__ __noinline__ void seq_fill(const DevSys& s, int64_t p, int64_t k0, int64_t cnt, double* out,
+                                      double* acc_last)
+{
+    int kind;
+    int64_t ko;
+    uint64_t sto;
+    seq_origin(s, p, kind, ko, sto);
+    int64_t k1 = k0 + cnt;
+    double acc_out = 0.0;
+    if (kind) {
+        double yr = s.anc_val[p];
+        if (k1 > ko) {
+            double y = yr;
+            uint64_t st = sto;
+            if (ko >= k0) {
+                out[ko - k0] = y;
+            }
+            for (int64_t k = ko + 1; k < k1; ++k) {
+                st = pcg_step(st);
+                y = FQ_ADD(y, dev_draw(s, st));
+                if (k >= k0) {
+                    out[k - k0] = y;
+                }
+            }
+            if (k1 - 1 >= ko) {
+                acc_out = y;
+            }
+        }
+        if (k0 < ko) {
+            double y = yr;
+            uint64_t st = sto;
+            for (int64_t k = ko - 1; k >= k0; --k) {
+                y = FQ_SUB(y, dev_draw(s, st));
+                if (k < k1) {
+                    out[k - k0] = y;
+                    if (k == k1 - 1) {
+                        acc_out = y;
+                    }
+                }
+                st = pcg_advance(st, ~0ULL);
+            }
+        }
+    }
+    else {
+        int64_t n0 = s.n0;
+        double o = off_of(s, p);
+        if (k1 > 0) {
+            uint64_t st = sto;
+            double c = 0.0, y = 0.0;
+            for (int64_t k = 0; k < k1; ++k) {
+                double d = dev_draw(s, st);
+                if (k == 0) {
+                    c = d;
+                    y = FQ_ADD(c, o);
+                }
+                else if (k < n0) {
+                    c = FQ_ADD(c, d);
+                    y = FQ_ADD(c, o);
+                }
+                else {
+                    y = FQ_ADD(y, d);
+                }
+                if (k >= k0) {
+                    out[k - k0] = y;
+                }
+                st = pcg_step(st);
+            }
+            acc_out = (k1 - 1 < n0) ? c : y;
+        }
+        if (k0 < 0) {
+            double y = FQ_ADD(dev_draw(s, sto), o);
+            uint64_t st = sto;
+            for (int64_t k = -1; k >= k0; --k) {
+                y = FQ_SUB(y, dev_draw(s, st));
+                if (k < k1) {
+                    out[k - k0] = y;
+                    if (k == k1 - 1) {
+                        acc_out = y;
+                    }
+                }
+                st = pcg_advance(st, ~0ULL);
+            }
+        }
+    }
+    if (acc_last) {
+        *acc_last = acc_out;
+    }
+}
+
+/* Forward walker over the canonical sequence, valid at indices >= the origin. */
+struct Walker {
+    int64_t k;   /* index of the last produced value */
+    double acc;  /* accumulator at k (c_k in the initial region, else y_k) */
+    double y;    /* y_k */
+    uint64_t st; /* pcg32 state whose output is d_{k+1} */
+    int kind;
+    int64_t n0;
+    double o;
+};
+
+__device__ __forceinline__ void walker_next(const DevSys& s, Walker& w)
+{
+    double d = dev_draw(s, w.st);
+    w.st = pcg_step(w.st);
+    int64_t k = w.k + 1;
+    if (w.kind) {
+        w.acc = FQ_ADD(w.acc, d);
+        w.y = w.acc;
+    }
+    else if (k < w.n0) {
+        w.acc = FQ_ADD(w.acc, d);
+        w.y = FQ_ADD(w.acc, w.o);
+    }
+    else if (k == w.n0) {
+        w.y = FQ_ADD(FQ_ADD(w.acc, w.o), d);
+        w.acc = w.y;
+    }
+    else {
+        w.acc = FQ_ADD(w.acc, d);
+        w.y = w.acc;
+    }
+    w.k = k;
+}
+
+/* Refresh the cached well of particle p from its chunk row at chunk index li. */
+__device__ __forceinline__ double4_32a make_wc(const DevSys& s, double yl, double yr)
+{
+    double4_32a w;
+    w.x = yl;
+    w.y = yr;
+    if (s.pot == POT_SEMISMOOTH) {
+        double xi = FQ_MUL(0.5, FQ_ADD(yl, yr));
+        double den = FQ_ADD(s.mu, s.kappa);
+        w.z = FQ_DIV(FQ_ADD(FQ_MUL(s.mu, xi), FQ_MUL(s.kappa, yl)), den); /* u_l */
+        w.w = FQ_DIV(FQ_ADD(FQ_MUL(s.mu, xi), FQ_MUL(s.kappa, yr)), den); /* u_r */
+    }
+    else {
+        w.z = FQ_MUL(0.5, FQ_ADD(yl, yr)); /* well centre */
+        w.w = FQ_MUL(0.5, FQ_SUB(yr, yl)); /* half width (Smooth) */
+    }
+    return w;
+}
+
+/*
+ * prrng align for particle p at target u: find i with y[i] <= u < y[i+1]; when i leaves
+ * [min_margin, W - buffer) move the window so that the target sits at chunk index `margin`.
+ * Updates start, cidx, gidx, wc, acc_end of the particle.  Returns false for a non-finite u
+ * (the index is then kept; the NaN is reported by the step's NaN check).
+ */
+static __device__ __noinline__ bool dev_align(const DevSys& s, int64_t p, double u)
+{
+    if (!(u == u) || fabs(u) == __longlong_as_double(0x7ff0000000000000LL)) {
+        return false;
+    }
+    const int64_t W = s.W;
+    double* y = s.data + p * W;
+    int64_t start = s.start[p];
+    int64_t li = s.cidx[p];
+    int64_t gi;
+    int kind;
+    int64_t ko;
+    uint64_t sto;
+    seq_origin(s, p, kind, ko, sto);
+    if (y[0] <= u && u < y[W - 1]) {
+        if (y[li] <= u) {
+            while (li + 1 < W && y[li + 1] <= u) {
+                ++li;
+            }
+        }
+        else {
+            while (li > 0 && y[li] > u) {
+                --li;
+            }
+        }
+        if (li >= s.min_margin && li < W - s.buffer) {
+            s.cidx[p] = (int32_t)li;
+            s.gidx[p] = start + li;
+            s.wc[p] = make_wc(s, y[li], y[li + 1]);
+            return true;
+        }
+        gi = start + li;
+    }
+    else if (u >= y[W - 1]) {
+        gi = -1; /* found below */
+    }
+    else {
+        gi = -2;
+    }
+
+    int64_t end = start + W - 1;
+    bool fast = end >= ko; /* the forward walker is exact from the window end */
+    if (gi == -1) {
+        if (fast) {
+            Walker w;
+            w.k = end;
+            w.acc = s.acc_end[p];
+            w.y = y[W - 1];
+            w.st = pcg_advance(sto, (uint64_t)(end + 1 - ko));
+            w.kind = kind;
+            w.n0 = s.n0;
+            w.o = off_of(s, p);
+            for (int64_t it = 0;; ++it) {
+                if (it >= MAX_WALK) {
+                    atomicOr(&s.ctl->walk_flag, 1);
+                    return false;
+                }
+                walker_next(s, w);
+                if (w.y > u) {
+                    gi = w.k - 1;
+                    break;
+                }
+            }
+        }
+        else {
+            /* window lies left of the origin: scan forward block by block by replay */
+            int64_t k = end;
+            for (int64_t it = 0;; ++it) {
+                if (it * 64 >= MAX_WALK) {
+                    atomicOr(&s.ctl->walk_flag, 1);
+                    return false;
+                }
+                double blk[64];
+                seq_fill(s, p, k + 1, 64, blk, nullptr);
+                int64_t j = 0;
+                while (j < 64 && blk[j] <= u) {
+                    ++j;
+                }
+                if (j < 64) {
+                    gi = k + j;
+                    break;
+                }
+                k += 64;
+            }
+        }
+    }
+    else if (gi == -2) {
+        int64_t k = start; /* y_k > u */
+        for (int64_t it = 0;; ++it) {
+            if (it * 64 >= MAX_WALK) {
+                atomicOr(&s.ctl->walk_flag, 1);
+                return false;
+            }
+            double blk[64];
+            seq_fill(s, p, k - 64, 64, blk, nullptr);
+            int64_t j = 63;
+            while (j >= 0 && blk[j] > u) {
+                --j;
+            }
+            if (j >= 0) {
+                gi = k - 64 + j;
+                break;
+            }
+            k -= 64;
+        }
+    }
+
+    int64_t ns = gi - s.margin;
+    double acc = 0.0;
+    if (ns > start && fast) {
+        /* forward move: keep the overlap, extend by the walker from the old window end */
+        int64_t keep = end + 1 - ns; /* values of the old window that stay (may be <= 0) */
+        if (keep > 0) {
+            for (int64_t j = 0; j < keep; ++j) {
+                y[j] = y[j + (ns - start)];
+            }
+        }
+        Walker w;
+        w.k = end;
+        w.acc = s.acc_end[p];
+        w.y = 0.0;
+        w.st = pcg_advance(sto, (uint64_t)(end + 1 - ko));
+        w.kind = kind;
+        w.n0 = s.n0;
+        w.o = off_of(s, p);
+        int64_t first = keep > 0 ? keep : 0;
+        while (w.k < ns + first - 1) {
+            walker_next(s, w);
+        }
+        for (int64_t j = first; j < W; ++j) {
+            walker_next(s, w);
+            y[j] = w.y;
+        }
+        acc = w.acc;
+    }
+    else {
+        seq_fill(s, p, ns, W, y, &acc);
+    }
+    s.start[p] = ns;
+    s.acc_end[p] = acc;
+    li = s.margin;
+    s.cidx[p] = (int32_t)li;
+    s.gidx[p] = ns + li;
+    s.wc[p] = make_wc(s, y[li], y[li + 1]);
+    return true;
+}
+
+/* Potential force, Cuspy detail.h:139-170 / SemiSmooth :236-277 / Smooth :379-409. */
+template <int POT, bool UNIT_MU>
+__device__ __forceinline__ double pot_force(const DevSys& s, const double4_32a& w, double up)
+{
+    if (POT == POT_CUSPY) {
+        double f = FQ_SUB(w.z, up);
+        return UNIT_MU ? f : FQ_MUL(f, s.mu);
+    }
+    else if (POT == POT_SEMISMOOTH) {
+        if (up < w.z) {
+            return FQ_MUL(s.kappa, FQ_SUB(up, w.x));
+        }
+        else if (up <= w.w) {
+            return FQ_MUL(s.mu, FQ_SUB(FQ_MUL(0.5, FQ_ADD(w.x, w.y)), up));
+        }
+        return FQ_MUL(s.kappa, FQ_SUB(up, w.y));
+    }
+    else {
+        const double pi = 3.14159265358979323846;
+        double arg = FQ_DIV(FQ_MUL(pi, FQ_SUB(up, w.z)), w.w);
+        return FQ_MUL(FQ_DIV(FQ_MUL(-s.mu, w.w), pi), fq_sin(arg));
+    }
+}
+
+/* ------------------------------------------------ canonical reductions */
+
+/* Sum over the 32 lanes in the fixed pairwise order (lane i with i^1, then pairs of pairs, ...). */
+__device__ __forceinline__ double warp_tree(double x)
+{
+#pragma unroll
+    for (int m = 1; m < 32; m <<= 1) {
+        double y = __shfl_xor_sync(0xffffffffu, x, m);
+        x = (threadIdx.x & m) ? FQ_ADD(y, x) : FQ_ADD(x, y);
+    }
+    return x;
+}
+
+/* Pairwise tree over the threads of a CTA (blockDim a power of two, <= 1024), thread t holding the
+ * sum of the t-th aligned subtree.  Result valid in thread 0.  sh needs blockDim/32 doubles. */
+__device__ __forceinline__ double cta_tree(double x, double* sh)
+{
+    x = warp_tree(x);
+    int nw = blockDim.x >> 5;
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) {
+        sh[wid] = x;
+    }
+    __syncthreads();
+    if (wid == 0) {
+        double y = lane < nw ? sh[lane] : 0.0;
+        /* pairwise over the nw warp sums (pad with zeros to 32 lanes: x + 0 is exact) */
+        y = warp_tree(y);
+        x = y;
+    }
+    return x;
+}
+
+/* Pairwise sum of v[lo .. lo+len) with len a power of two (binary-counter order == recursive tree). */
+template <class F>
+__device__ __forceinline__ double serial_tree(F get, int64_t lo, int64_t len)
+{
+    double st[40];
+    for (int64_t i = 0; i < len; ++i) {
+        double x = get(lo + i);
+        int64_t j = i;
+        int lvl = 0;
+        while (j & 1) {
+            x = FQ_ADD(st[lvl], x);
+            j >>= 1;
+            ++lvl;
+        }
+        st[lvl] = x;
+    }
+    int lvl = 0;
+    while ((int64_t(1) << lvl) < len) {
+        ++lvl;
+    }
+    return st[lvl];
+}
+
+__host__ __device__ __forceinline__ int64_t next_pow2(int64_t n)
+{
+    int64_t p = 1;
+    while (p < n) {
+        p <<= 1;
+    }
+    return p;
+}
+
+} // namespace fqsb
+
+#endif

@@ -1,0 +1,160 @@
+/*
+ * fqsb.h -- C ABI of the GB300-native FrictionQPotSpringBlock time-integration path.
+ *
+ * One opaque handle owns one system (a Line1d / Line2d / Particles System_*
+ * of the reference) resident in device memory.  Every entry point is
+ * synchronous at return, takes plain pointers and sizes (host memory unless
+ * the name ends in _device), and returns an fqsb_status; the message of the
+ * last failure is available from fqsb_last_error().  Error texts reproduce
+ * the reference's exceptions ("NaN entries found", "No convergence found",
+ * "Operation not possible.").
+ *
+ * Each declaration names the reference interface it replaces, as
+ * file:line inside the reference project (python/main.cpp is the pybind11
+ * boundary; include/FrictionQPotSpringBlock/detail.h holds the C++ methods).
+ */
+#ifndef FQSB_H
+#define FQSB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct fqsb_system fqsb_system;
+
+typedef enum {
+    FQSB_OK = 0,
+    FQSB_ERR_NAN = 1,            /* "NaN entries found"          detail.h:1567-1569 */
+    FQSB_ERR_NO_CONVERGENCE = 2, /* "No convergence found"       detail.h:1787-1789 */
+    FQSB_ERR_INVALID = 3,        /* invalid argument / shape */
+    FQSB_ERR_CUDA = 4,           /* CUDA runtime error */
+    FQSB_ERR_TIMEOUT = 5,        /* a bounded device wait ran out */
+    FQSB_ERR_NOT_POSSIBLE = 6,   /* "Operation not possible."    detail.h:414-422 */
+    FQSB_ERR_REQUIRE = 7,        /* FRICTIONQPOTSPRINGBLOCK_REQUIRE failed, detail.h:1992-1994 */
+    FQSB_ERR_UNSUPPORTED = 8,    /* distribution not implemented on the device */
+    FQSB_ERR_NO_DEVICE = 9       /* no CUDA device available */
+} fqsb_status;
+
+/* potential (detail.h:113 Cuspy, :212 SemiSmooth, :356 Smooth) */
+enum { FQSB_CUSPY = 0, FQSB_SEMISMOOTH = 1, FQSB_SMOOTH = 2 };
+/* interactions (none = Particles.h:93-311; detail.h:446 Laplace1d; :524 Laplace2d) */
+enum { FQSB_INTERACTIONS_NONE = 0, FQSB_LAPLACE1D = 1, FQSB_LAPLACE2D = 2 };
+/* distributions, prrng names (detail.h:31-66) */
+enum {
+    FQSB_DIST_RANDOM = 0,
+    FQSB_DIST_DELTA = 1,
+    FQSB_DIST_EXPONENTIAL = 2,
+    FQSB_DIST_POWER = 3,
+    FQSB_DIST_GAMMA = 4,
+    FQSB_DIST_PARETO = 5,
+    FQSB_DIST_WEIBULL = 6,
+    FQSB_DIST_NORMAL = 7
+};
+/* per-particle fields (main.cpp:80-127) */
+enum {
+    FQSB_FIELD_U = 0,
+    FQSB_FIELD_V = 1,
+    FQSB_FIELD_A = 2,
+    FQSB_FIELD_F = 3,
+    FQSB_FIELD_F_POTENTIAL = 4,
+    FQSB_FIELD_F_INTERACTIONS = 5,
+    FQSB_FIELD_F_FRAME = 6,
+    FQSB_FIELD_F_DAMPING = 7
+};
+/* scalars */
+enum {
+    FQSB_SCALAR_U_FRAME = 0,     /* main.cpp:104 */
+    FQSB_SCALAR_T = 1,           /* main.cpp:103 */
+    FQSB_SCALAR_TEMPERATURE = 2, /* main.cpp:128, detail.h:1500-1503 */
+    FQSB_SCALAR_RESIDUAL = 3,    /* main.cpp:129, detail.h:1512-1520 */
+    FQSB_SCALAR_MEAN_F_FRAME = 4 /* xt::mean(f_frame), detail.h:1991 */
+};
+
+/*
+ * Construction parameters.  Replaces the constructors
+ *   Line1d::System_Cuspy_Laplace       main.cpp:493-520, Line1d.h:134-161
+ *   Line1d::System_SemiSmooth_Laplace  main.cpp:684-713, Line1d.h:348-376
+ *   Line1d::System_Smooth_Laplace      main.cpp:729-756, Line1d.h:394-421
+ *   Line2d::System_Cuspy_Laplace       main.cpp:924-951, Line2d.h:88-115
+ *   Particles::System_{Cuspy,SemiSmooth,Smooth}  Particles.h:93-311
+ */
+typedef struct {
+    int potential;           /* FQSB_CUSPY / FQSB_SEMISMOOTH / FQSB_SMOOTH */
+    int interactions;        /* FQSB_INTERACTIONS_NONE / FQSB_LAPLACE1D / FQSB_LAPLACE2D */
+    int64_t rows, cols;      /* 1d: rows = 1, cols = N */
+    double m, eta, mu, kappa, k_interactions, k_frame, dt;
+    uint64_t seed;           /* particle p uses pcg32(initstate = seed + p, initseq = 0) */
+    int distribution;        /* FQSB_DIST_* */
+    int n_parameters;        /* <= 4 */
+    double parameters[4];
+    double offset;           /* global shift of the yield positions (Line1d.h:157) */
+    const double* offset_per_particle; /* extension, may be NULL: per-particle shift replacing `offset` */
+    int64_t nchunk;          /* yield positions held per particle (>= 34) */
+    void* stream;            /* cudaStream_t to run on, or NULL for a private stream */
+    int device;              /* CUDA device ordinal */
+} fqsb_config;
+
+/* Lifecycle. */
+int fqsb_create(const fqsb_config* cfg, fqsb_system** out);
+int fqsb_destroy(fqsb_system* h);
+const char* fqsb_last_error(const fqsb_system* h); /* h may be NULL: last error of fqsb_create */
+int fqsb_size(const fqsb_system* h, int64_t* n);
+
+/* Dynamics. */
+int fqsb_time_step(fqsb_system* h);                               /* timeStep         main.cpp:212, detail.h:1539 */
+int fqsb_time_steps(fqsb_system* h, uint64_t n);                  /* timeSteps        main.cpp:213, detail.h:1577 */
+int fqsb_flow_steps(fqsb_system* h, uint64_t n, double v_frame);  /* flowSteps        main.cpp:224, detail.h:1637 */
+int fqsb_time_steps_until_event(fqsb_system* h, double tol, uint64_t niter_tol, uint64_t max_iter,
+                                uint64_t* ret);                    /* timeStepsUntilEvent main.cpp:215-222, detail.h:1595 */
+int fqsb_minimise(fqsb_system* h, double tol, uint64_t niter_tol, uint64_t max_iter, int time_activity,
+                  int max_iter_is_error, uint64_t* ret);           /* minimise         main.cpp:161-170, detail.h:1676 */
+int fqsb_minimise_truncate(fqsb_system* h, const int64_t* i_n, uint64_t A_truncate, uint64_t S_truncate, double tol,
+                           uint64_t niter_tol, uint64_t max_iter, int time_activity, int max_iter_is_error,
+                           uint64_t* ret);                         /* minimise_truncate main.cpp:172-184, detail.h:1833 */
+int fqsb_max_uniform_displacement(fqsb_system* h, int direction, double* ret); /* main.cpp:136-141, detail.h:1901 */
+int fqsb_event_driven_step(fqsb_system* h, double eps, int kick, int direction,
+                           double* ret);                           /* eventDrivenStep  main.cpp:186-193, detail.h:1933 */
+int fqsb_trigger(fqsb_system* h, int64_t p, double eps, int direction); /* trigger     main.cpp:143-150, detail.h:1972 */
+int fqsb_advance_to_fixed_force(fqsb_system* h, double f_frame, int allow_plastic); /* main.cpp:152-158, detail.h:1988 */
+int fqsb_quench(fqsb_system* h);                                  /* quench           main.cpp:131, detail.h:1527 */
+int fqsb_refresh(fqsb_system* h);                                 /* refresh          main.cpp:130, detail.h:1310 */
+
+/* State transfer (host buffers of size N, C order). */
+int fqsb_get_field(fqsb_system* h, int field, double* out);       /* u/v/a/f/f_* getters main.cpp:80-127 */
+int fqsb_set_field(fqsb_system* h, int field, const double* in);  /* u/v/a setters main.cpp:80-99, detail.h:1231-1259 */
+int fqsb_get_scalar(fqsb_system* h, int which, double* out);
+int fqsb_set_u_frame(fqsb_system* h, double u_frame);             /* u_frame setter main.cpp:104, detail.h:1253 */
+int fqsb_get_inc(fqsb_system* h, int64_t* inc);                   /* inc getter main.cpp:102 */
+int fqsb_set_inc(fqsb_system* h, int64_t inc);                    /* inc setter main.cpp:102, detail.h:1212 */
+int fqsb_set_t(fqsb_system* h, double t);                         /* t setter main.cpp:103, detail.h:1200 */
+int fqsb_quasistatic_activity(fqsb_system* h, int64_t* first, int64_t* last); /* main.cpp:195-201, detail.h:1802-1818 */
+
+/* Chunk (prrng pcg32_tensor_cumsum members used through system.chunk, tests/test_Line1d.py:83-86,309-341). */
+int fqsb_get_index(fqsb_system* h, int64_t* index_at_align, int64_t* chunk_index_at_align, double* left_of_align,
+                   double* right_of_align);                        /* any pointer may be NULL */
+int fqsb_chunk_size(fqsb_system* h, int64_t* nchunk);
+int fqsb_chunk_data(fqsb_system* h, double* data, int64_t* start); /* data [N, nchunk]; either may be NULL */
+int fqsb_chunk_state_at(fqsb_system* h, const int64_t* index, uint64_t* state);
+int fqsb_chunk_restore(fqsb_system* h, const uint64_t* state, const double* value, const int64_t* index);
+
+/*
+ * Device-resident variants for callers that keep data on the GPU (pointers
+ * are device pointers of N doubles on the handle's device).
+ */
+int fqsb_get_field_device(fqsb_system* h, int field, double* out_device);
+int fqsb_set_field_device(fqsb_system* h, int field, const double* in_device);
+
+/* Timing support: the stream the handle launches on (a cudaStream_t). */
+int fqsb_get_stream(fqsb_system* h, void** stream);
+
+/* Build information: "fqsb <version> sm_103a". */
+const char* fqsb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

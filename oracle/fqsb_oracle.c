@@ -1183,3 +1183,38 @@ int oq_advance_to_fixed_force(oq_system* s, double f_frame, int allow_plastic)
     }
     return OQ_OK;
 }
+
+/* Canonical yield sequence of one particle p of a freshly constructed system, without building
+ * the system: y_k for k in [k0, k0+count).  Used for spot checks at full problem sizes. */
+int oq_sequence(uint64_t seed, int64_t p, int distribution, const double* parameters, int n_parameters, double offset,
+                int64_t nchunk, int math_mode, int64_t k0, int64_t count, double* out)
+{
+    if (!dist_supported(distribution) || n_parameters > 4 || nchunk < 1) {
+        return OQ_ERR_INVALID;
+    }
+    oq_system s;
+    memset(&s, 0, sizeof(s));
+    s.N = 1;
+    s.n = nchunk;
+    s.dist = distribution;
+    s.npar = n_parameters;
+    for (int i = 0; i < n_parameters; ++i) {
+        s.par[i] = parameters[i];
+    }
+    s.offset = offset;
+    s.math_mode = math_mode;
+    uint64_t g0, inc;
+    int restored = 0;
+    int64_t kr = 0;
+    uint64_t sr = 0;
+    double yr = 0.0;
+    pcg_seed(seed + (uint64_t)p, 0u, &g0, &inc);
+    s.g0 = &g0;
+    s.inc = &inc;
+    s.restored = &restored;
+    s.kr = &kr;
+    s.sr = &sr;
+    s.yr = &yr;
+    seq_fill(&s, 0, k0, count, out);
+    return OQ_OK;
+}

@@ -92,6 +92,8 @@ int oq_chunk_data(oq_system* s, double* out, int64_t* start);
 int oq_chunk_state_at(oq_system* s, const int64_t* index, uint64_t* state);
 int oq_chunk_restore(oq_system* s, const uint64_t* state, const double* value, const int64_t* index);
 int oq_yield_sequence(oq_system* s, int64_t p, int64_t k0, int64_t count, double* out);
+int oq_sequence(uint64_t seed, int64_t p, int distribution, const double* parameters, int n_parameters, double offset,
+                int64_t nchunk, int math_mode, int64_t k0, int64_t count, double* out);
 int64_t oq_quasistatic_first(oq_system* s);
 int64_t oq_quasistatic_last(oq_system* s);
 

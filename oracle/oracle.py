@@ -96,6 +96,7 @@ def lib():
         L.oq_chunk_state_at.argtypes = [P, P, P]
         L.oq_chunk_restore.argtypes = [P, P, P, P]
         L.oq_yield_sequence.argtypes = [P, i64, i64, i64, P]
+        L.oq_sequence.argtypes = [u64, i64, i32, pd, i32, d, i64, i32, i64, i64, P]
         L.oq_quasistatic_first.restype = i64
         L.oq_quasistatic_first.argtypes = [P]
         L.oq_quasistatic_last.restype = i64
@@ -136,6 +137,17 @@ def transform(distribution: str, parameters, r32: int, math_mode: int = MATH_POR
 
 def math(which: str, x: float, y: float = 0.0, math_mode: int = MATH_PORTABLE) -> float:
     return lib().oq_math({"log": 0, "pow": 1, "sin": 2, "exp": 3}[which], x, y, math_mode)
+
+
+def sequence(seed, p, distribution, parameters, offset, nchunk, k0, count, math_mode=MATH_PORTABLE):
+    """Canonical yield positions y_k, k in [k0, k0+count), of particle p of a fresh system."""
+    par = (ctypes.c_double * 4)(*list(parameters))
+    out = np.empty(count)
+    rc = lib().oq_sequence(int(seed), int(p), DISTRIBUTIONS[distribution], par, len(parameters), float(offset),
+                           int(nchunk), math_mode, int(k0), int(count), _ptr(out))
+    if rc:
+        raise OracleError("invalid sequence request")
+    return out
 
 
 class OracleError(RuntimeError):
