@@ -1,0 +1,349 @@
+"""Benchmark of the GB300 time-integration path (and of the CPU reference arm).
+
+Workload (the large-N throughput configuration): Line1d System_Cuspy_Laplace,
+N = 2^22 particles on a periodic ring, m = 1, eta = 0.1, mu = 1,
+k_interactions = 1, k_frame = 1/N, dt = 0.1; yield distances Weibull(k=2,
+scale=1) + 1e-5 from pcg32 (seed 1, particle p on stream initstate = 1 + p),
+2000 yield positions per particle; initial u ~ N(0, 0.1^2) (numpy PCG64,
+seed 1), v = 0.  The frame is ramped by 1e-4 per time step
+(flowSteps with v_frame = 1e-3), then jumps by +0.5, then minimise(tol=1e-5).
+
+One bench step = flowSteps(1000): 1000 fused time steps over all particles,
+so --steps 10 covers the configuration's 10^4 steps.  The metric is
+particle-steps/s (FP64).  After the timed steps the +0.5 jump and minimise are
+run once and their wall time is reported (minimise_s).
+
+`value` times the device-resident steps (state already in HBM); `e2e` times
+the same steps through the public API with host buffers: each step copies u
+and v from pinned host memory into the system, runs flowSteps(1000) and reads
+u back.  `--impl reference` times the CPU reference path instead (the CPU
+oracle, a loop-per-statement restatement of the reference, on the host
+cores), on bounded samples of the same workload.
+
+Multi-GPU (torchrun): the plain path does not shard (one system fits one GPU),
+so every rank runs an independent replica (weak scaling); value = sum of the
+ranks' particle-steps / max rank time.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N_DEFAULT = 2 ** 22
+INNER = 1000
+METRIC = "particle-steps/s (FP64)"
+PAR = dict(m=1.0, eta=0.1, mu=1.0, k_interactions=1.0, dt=0.1, seed=1, distribution="weibull",
+           parameters=[2.0, 1.0, 1e-5], offset=-100.0, nchunk=2000)
+V_FRAME = 1e-3  # u_frame += v_frame * dt = 1e-4 per step
+BYTES_PER_PARTICLE_STEP = 64  # read+write u, v, a (48 B) + read the current well {y_left, y_right} (16 B)
+FP64_OPS_PER_PARTICLE_STEP = 29  # 26 add/mul of the exact-order step (unit m, mu, k) + 3 compares
+
+
+def workload(n):
+    return (f"Line1d System_Cuspy_Laplace N={n} ring, m=1 eta=0.1 mu=1 k=1 k_frame=1/N dt=0.1, "
+            f"weibull(2,1)+1e-5 nchunk=2000 seed=1, u0~N(0,0.1^2); step = flowSteps({INNER}, v_frame=1e-3) "
+            f"(u_frame +1e-4 per time step); then u_frame += 0.5 and minimise(tol=1e-5)")
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index=0):
+        self.dev = device_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in pathlib.Path(self.path).read_text().splitlines():
+            cols = [c.strip() for c in line.split(",")]
+            if len(cols) < 9:
+                continue
+            try:
+                sm.append(float(cols[1]))
+                smax.append(float(cols[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, cols[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline_sample(n_sample=2 ** 16, steps=3000, repeats=1):
+    """Time the CPU oracle (loop-per-statement restatement of the reference, libm, sequential sums)
+    on a bounded sample of the same workload: the first n_sample particles' parameters on a ring of
+    n_sample, flowSteps(steps).  Returns particle-steps/s on one core."""
+    from oracle import oracle as O
+
+    s = O.line1d("Cuspy", shape=[n_sample], k_frame=1.0 / n_sample, **PAR, sum_mode=O.SUM_SEQUENTIAL,
+                 math_mode=O.MATH_LIBM)
+    s.u = np.random.default_rng(1).normal(0.0, 0.1, N_DEFAULT)[:n_sample]
+    s.flowSteps(20, V_FRAME)
+    t0 = time.perf_counter()
+    for _ in range(repeats):
+        s.flowSteps(steps, V_FRAME)
+    dt = time.perf_counter() - t0
+    return n_sample * steps * repeats / dt, dt
+
+
+def _ref_worker(args):
+    n_sample, steps, nsteps_total, warm = args
+    from oracle import oracle as O
+
+    s = O.line1d("Cuspy", shape=[n_sample], k_frame=1.0 / n_sample, **PAR, sum_mode=O.SUM_SEQUENTIAL,
+                 math_mode=O.MATH_LIBM)
+    s.u = np.random.default_rng(1).normal(0.0, 0.1, n_sample)
+    for _ in range(warm):
+        s.flowSteps(steps, V_FRAME)
+    times = []
+    for _ in range(nsteps_total):
+        t0 = time.perf_counter()
+        s.flowSteps(steps, V_FRAME)
+        times.append(time.perf_counter() - t0)
+    return times
+
+
+def run_reference(args, rank, world):
+    """CPU reference arm: the reference path restated on the host (the reference's own build needs
+    prrng / xtensor / GooseFEM, absent here), one independent sample system per host core."""
+    if rank != 0:
+        return
+    import multiprocessing as mp
+
+    from oracle import oracle as O
+
+    O.build()
+    cores = os.cpu_count() or 1
+    n_sample, steps = 2 ** 14, 200
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_ref_worker, [(n_sample, steps, args.steps, args.warmup)] * cores)
+    per_step = [max(r[i] for r in res) for i in range(args.steps)]
+    total_time = sum(per_step)
+    value = cores * n_sample * steps * args.steps / total_time
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": "particle-steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * total_time / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": workload(args.n), "l2": "inputs larger than L2 on the GPU arm"},
+        "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+                         "sample": f"{cores} independent systems of N={n_sample} (one per core), "
+                                   f"each step flowSteps({steps}); the reference's path restated in C "
+                                   "(oracle/), built -O2 -ffp-contract=off"},
+        "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--nchunk", type=int, default=2000, help="yield positions per particle (profiling cases only)")
+    ap.add_argument("--no-minimise", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+
+    import frictionqpotspringblock_gb300 as fqsb
+
+    N = args.n
+    par = dict(PAR)
+    par["nchunk"] = args.nchunk
+    system = fqsb.Line1d.System_Cuspy_Laplace(k_frame=1.0 / N, shape=[N], device=local_rank, **par)
+    u0 = np.random.default_rng(1).normal(0.0, 0.1, N)
+    system.u = u0
+    stream = torch.cuda.ExternalStream(system.stream)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    for _ in range(args.warmup):
+        system.flowSteps(INNER, V_FRAME)
+
+    # ---- device-resident timed region
+    clocks = ClockSampler(local_rank)
+    barrier()
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    t_wall0 = time.perf_counter()
+    e0.record(stream)
+    for _ in range(args.steps):
+        system.flowSteps(INNER, V_FRAME)
+    e1.record(stream)
+    barrier()
+    t_wall = time.perf_counter() - t_wall0
+    clk = clocks.stop()
+    dev_s = max_over_ranks(e0.elapsed_time(e1) / 1e3)
+    launches = args.steps * INNER
+    particle_steps = N * INNER * args.steps
+    value = world * particle_steps / dev_s
+    kernel_s = dev_s / launches
+    hbm_peak, peak_kind = peaks()
+    achieved_gbs = BYTES_PER_PARTICLE_STEP * N / kernel_s / 1e9
+
+    # ---- end-to-end through the public API with host buffers
+    host_u = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
+    host_v = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
+    host_u[:] = system.u
+    host_v[:] = system.v
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        system.u = host_u
+        system.v = host_v
+        system.flowSteps(INNER, V_FRAME)
+        out = system.u
+    barrier()
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e_value = world * particle_steps / e2e_s
+    del out
+
+    # ---- the frame jump and minimise of the configuration (timed once)
+    minimise = None
+    if not args.no_minimise:
+        system.u_frame = system.u_frame + 0.5
+        barrier()
+        t0 = time.perf_counter()
+        inc0 = system.inc
+        ret = system.minimise(tol=1e-5)
+        barrier()
+        minimise = {"seconds": time.perf_counter() - t0, "steps": system.inc - inc0, "ret": ret}
+
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu_baseline:
+        v, secs = cpu_baseline_sample()
+        cpu = {"value": v, "unit": "particle-steps/s", "cores": 1, "kind": "port",
+               "sample": f"oracle (reference restated in C, loop per statement, libm, sequential sums), "
+                         f"N=65536 ring of the same parameters, flowSteps(3000), {secs:.1f} s on 1 core"}
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "particle-steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * dev_s / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": workload(N), "particles": N, "time_steps_per_step": INNER,
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (state + well cache ~270 MB vs 129 MB L2), no flush"},
+        "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": 2 * 8 * N,
+                "d2h_bytes_per_step": 8 * N},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved_gbs / hbm_peak, "traffic": None, "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_particle_step": BYTES_PER_PARTICLE_STEP,
+                     "kernel": "k_step_line<Cuspy, Laplace1d, units, 2 per thread>",
+                     "kernel_us": kernel_s * 1e6},
+        "fp64": {"ops_per_particle_step": FP64_OPS_PER_PARTICLE_STEP,
+                 "achieved_gops": FP64_OPS_PER_PARTICLE_STEP * N / kernel_s / 1e9,
+                 "peak_gops": 505.0, "peak_source": "profiles/fp64_throughput_gb300.md",
+                 "frac": FP64_OPS_PER_PARTICLE_STEP * N / kernel_s / 1e9 / 505.0},
+        "clocks": clk,
+        "wall_s": t_wall,
+        "minimise": minimise,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()
