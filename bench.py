@@ -49,7 +49,7 @@ PAR = dict(m=1.0, eta=0.1, mu=1.0, k_interactions=1.0, dt=0.1, seed=1, distribut
            parameters=[2.0, 1.0, 1e-5], offset=-100.0, nchunk=2000)
 V_FRAME = 1e-3  # u_frame += v_frame * dt = 1e-4 per step
 BYTES_PER_PARTICLE_STEP = 64  # read+write u, v, a (48 B) + read the current well {y_left, y_right} (16 B)
-FP64_OPS_PER_PARTICLE_STEP = 29  # 26 add/mul of the exact-order step (unit m, mu, k) + 3 compares
+FP64_OPS_PER_PARTICLE_STEP = 24  # fp64 add/mul of the exact-order step; compares and 2^k scalings run on the integer pipe
 
 
 def workload(n):

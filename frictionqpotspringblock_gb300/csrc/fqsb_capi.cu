@@ -12,6 +12,7 @@
  * reference does (set_u_frame recomputes f_frame and f, set_v / quench recompute f_damping
  * and f) until the next operation that calls updated_u.
  */
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -31,7 +32,6 @@ struct fqsb_system {
     cudaStream_t stream;
     bool own_stream;
     int device;
-    bool units;
     bool is2d;
     LineGeom lg;
     /* host mirrors of the run state */
@@ -125,9 +125,9 @@ __device__ __forceinline__ void pi_force(const DevSys& d, const double* u, int64
     double up = u[p];
     double4_32a w = d.wc[p];
     switch (d.pot) {
-        case POT_CUSPY: fp = pot_force<POT_CUSPY, false>(d, w, up); break;
-        case POT_SEMISMOOTH: fp = pot_force<POT_SEMISMOOTH, false>(d, w, up); break;
-        default: fp = pot_force<POT_SMOOTH, false>(d, w, up); break;
+        case POT_CUSPY: fp = pot_force<POT_CUSPY>(d, w, up); break;
+        case POT_SEMISMOOTH: fp = pot_force<POT_SEMISMOOTH>(d, w, up); break;
+        default: fp = pot_force<POT_SMOOTH>(d, w, up); break;
     }
     fi = 0.0;
     if (d.inter == INTER_LAPLACE1D) {
@@ -404,6 +404,33 @@ static uint64_t host_pcg_advance(uint64_t state, uint64_t delta)
 
 /* ------------------------------------------------------------ helpers */
 
+/* How the kernels multiply by a parameter c: skip for 1, exponent add for a positive normal power of
+ * two, fp64 multiply otherwise (all three give x * c exactly as IEEE multiplication does). */
+static Scale classify_scale(double c)
+{
+    Scale sc;
+    sc.c = c;
+    sc.e = 0;
+    sc.mode = SCALE_GENERAL;
+    if (c == 1.0) {
+        sc.mode = SCALE_ONE;
+        return sc;
+    }
+    int e = 0;
+    double m = std::frexp(c, &e);
+    if (c > 0.0 && m == 0.5 && std::isnormal(c)) {
+        sc.mode = SCALE_POW2;
+        sc.e = e - 1;
+    }
+    return sc;
+}
+
+/* state arrays are padded so that a CTA's vector loads of a partial last tile stay in bounds */
+static int64_t padded(int64_t n)
+{
+    return (n + 1023) / 1024 * 1024;
+}
+
 static double* cur_u(fqsb_system* h)
 {
     return h->d.u[h->cur];
@@ -488,35 +515,16 @@ static int materialise_forces(fqsb_system* h)
 
 /* ------------------------------------------------------------ run driver */
 
-static const int GRAPH_K = 64;
-
-static int launch_one_step(fqsb_system* h)
-{
-    cudaError_t e = h->is2d ? launch_step_grid(h->d, h->units, h->stream)
-                            : launch_step_line(h->d, h->lg, h->units, h->stream);
-    CU(h, e);
-    return FQSB_OK;
-}
+/* Device time after which a run's graph launch yields back to the host (which relaunches it). */
+static const uint64_t RUN_BUDGET_NS = 200ull * 1000ull * 1000ull;
+static const int64_t RING_MIN = 1024;
 
 static int ensure_graph(fqsb_system* h)
 {
     if (h->graph) {
         return FQSB_OK;
     }
-    cudaGraph_t g;
-    CU(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    for (int i = 0; i < GRAPH_K; ++i) {
-        cudaError_t e = h->is2d ? launch_step_grid(h->d, h->units, h->stream)
-                                : launch_step_line(h->d, h->lg, h->units, h->stream);
-        if (e != cudaSuccess) {
-            cudaStreamEndCapture(h->stream, &g);
-            return set_err(h, FQSB_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-        }
-    }
-    CU(h, cudaStreamEndCapture(h->stream, &g));
-    CU(h, cudaGraphInstantiate(&h->graph, g, 0));
-    cudaGraphDestroy(g);
-    h->graph_k = GRAPH_K;
+    CU(h, build_run_graph(h->d, h->lg, &h->graph));
     return FQSB_OK;
 }
 
@@ -527,8 +535,9 @@ struct RunResult {
 };
 
 /*
- * Run up to max_steps fused steps with the stop tests selected by flags; everything between
- * the host's upload of the control block and the read-back happens on the device.
+ * Run up to max_steps fused steps with the stop tests selected by flags.  The whole run is one
+ * launch of the run graph (a device-side loop); the host synchronises once (plus once per
+ * RUN_BUDGET_NS of device time for long runs).
  */
 static int run(fqsb_system* h, int64_t max_steps, int flags, double tol, int64_t niter_tol, double vdt,
                int64_t A_truncate, int64_t S_truncate, const int64_t* i_n_host, RunResult* res)
@@ -540,7 +549,21 @@ static int run(fqsb_system* h, int64_t max_steps, int flags, double tol, int64_t
         return FQSB_OK;
     }
     h->stored = false;
-    int rc = ensure_graph(h);
+    int rc;
+    if ((flags & RF_RESID) && niter_tol > h->ring_cap) {
+        if (h->d.ring) {
+            cudaFree(h->d.ring);
+        }
+        h->d.ring = nullptr;
+        CU(h, cudaMalloc(&h->d.ring, sizeof(double) * (size_t)niter_tol));
+        h->ring_cap = niter_tol;
+        if (h->graph) {
+            /* the ring pointer is a kernel argument of the graph */
+            cudaGraphExecDestroy(h->graph);
+            h->graph = nullptr;
+        }
+    }
+    rc = ensure_graph(h);
     if (rc) {
         return rc;
     }
@@ -557,31 +580,13 @@ static int run(fqsb_system* h, int64_t max_steps, int flags, double tol, int64_t
     c->cur = h->cur;
     c->inc = h->inc;
     c->u_frame = h->u_frame;
-    c->sl_pos = 0;
     c->sl_ge_tol = niter_tol;
     c->sl_ge_tol2 = niter_tol;
-    c->sl_asc = 0;
     c->init = 1;
     c->qs_first = h->qs_first;
     c->qs_last = h->qs_last;
+    c->budget_ns = RUN_BUDGET_NS;
     if ((flags & RF_RESID) && niter_tol > 0) {
-        if (h->ring_cap < niter_tol) {
-            if (h->d.ring) {
-                cudaFree(h->d.ring);
-            }
-            h->d.ring = nullptr;
-            CU(h, cudaMalloc(&h->d.ring, sizeof(double) * (size_t)niter_tol));
-            h->ring_cap = niter_tol;
-            /* the ring pointer is a kernel argument: re-capture the graph */
-            if (h->graph) {
-                cudaGraphExecDestroy(h->graph);
-                h->graph = nullptr;
-            }
-            rc = ensure_graph(h);
-            if (rc) {
-                return rc;
-            }
-        }
         k_fill<<<blocks_for(niter_tol, 128), 128, 0, h->stream>>>(h->d.ring, niter_tol, INFINITY);
         CU(h, cudaGetLastError());
     }
@@ -601,33 +606,19 @@ static int run(fqsb_system* h, int64_t max_steps, int flags, double tol, int64_t
                                                                     (long long*)&h->d.ctl->a_count);
         CU(h, cudaGetLastError());
     }
-    bool stop_tests = (flags & (RF_RESID | RF_EVENT | RF_TRUNCATE)) != 0;
-    int64_t launched = 0;
-    while (launched < max_steps) {
-        int64_t remaining = max_steps - launched;
-        if (remaining >= h->graph_k) {
-            CU(h, cudaGraphLaunch(h->graph, h->stream));
-            launched += h->graph_k;
+    for (;;) {
+        CU(h, cudaGraphLaunch(h->graph, h->stream));
+        CU(h, cudaMemcpyAsync(c, h->d.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, h->stream));
+        rc = sync(h);
+        if (rc) {
+            return rc;
         }
-        else {
-            for (int64_t i = 0; i < remaining; ++i) {
-                rc = launch_one_step(h);
-                if (rc) {
-                    return rc;
-                }
-            }
-            launched += remaining;
+        if (c->done || c->error) {
+            break;
         }
-        if (stop_tests || launched >= max_steps) {
-            CU(h, cudaMemcpyAsync(c, h->d.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, h->stream));
-            rc = sync(h);
-            if (rc) {
-                return rc;
-            }
-            if (c->done || c->error) {
-                break;
-            }
-        }
+        /* the launch used up its device-time budget: start a new launch window */
+        int64_t zero = 0;
+        CU(h, cudaMemcpyAsync(&h->d.ctl->launch_steps, &zero, sizeof(zero), cudaMemcpyHostToDevice, h->stream));
     }
     h->cur = c->cur;
     h->inc = c->inc;
@@ -680,6 +671,7 @@ static void free_all(fqsb_system* h)
     DevSys& d = h->d;
     void* ptrs[] = {d.data, d.start, d.cidx, d.gidx, d.wc, d.acc_end, d.anc_kind, d.anc_k, d.anc_state, d.anc_val,
                     d.u[0], d.u[1], d.v[0], d.v[1], d.a[0], d.a[1], d.ctl, d.ring, d.partials, d.i_n, d.sq2,
+                    d.cta_pending, d.regen_list,
                     (void*)d.offp, h->scratch, h->red_partials, h->red_out, h->mkey, h->mflag, h->fs[0], h->fs[1],
                     h->fs[2], h->fs[3], h->fs[4]};
     for (void* p : ptrs) {
@@ -793,9 +785,13 @@ extern "C" int fqsb_create(const fqsb_config* cfg, fqsb_system** out)
     d.margin = 30;
     d.min_margin = 6;
     h->is2d = cfg->interactions == FQSB_LAPLACE2D;
-    h->units = (cfg->mu == 1.0) && (d.k == 1.0 || cfg->interactions == FQSB_INTERACTIONS_NONE) && (d.inv_m == 1.0);
+    d.s_mu = classify_scale(d.mu);
+    d.s_k = classify_scale(d.k);
+    d.s_kf = classify_scale(d.k_frame);
+    d.s_im = classify_scale(d.inv_m);
     h->lg = line_geometry(N);
-    int64_t npart = h->is2d ? grid_reduce_ctas(N) : h->lg.grid;
+    int64_t nsteps_cta = step_ctas(d, h->lg);
+    int64_t npart = h->is2d ? std::max(grid_reduce_ctas(N), nsteps_cta) : h->lg.grid;
     d.npartials = npart;
 
 #define ALLOC(ptr, bytes)                                                                                \
@@ -809,6 +805,7 @@ extern "C" int fqsb_create(const fqsb_config* cfg, fqsb_system** out)
     } while (0)
 
     size_t nd = sizeof(double) * (size_t)N;
+    size_t ndp = sizeof(double) * (size_t)padded(N);
     ALLOC(d.data, sizeof(double) * (size_t)N * (size_t)d.W);
     ALLOC(d.start, sizeof(int64_t) * (size_t)N);
     ALLOC(d.cidx, sizeof(int32_t) * (size_t)N);
@@ -820,13 +817,17 @@ extern "C" int fqsb_create(const fqsb_config* cfg, fqsb_system** out)
     ALLOC(d.anc_state, sizeof(uint64_t) * (size_t)N);
     ALLOC(d.anc_val, nd);
     for (int b = 0; b < 2; ++b) {
-        ALLOC(d.u[b], nd);
-        ALLOC(d.v[b], nd);
-        ALLOC(d.a[b], nd);
+        ALLOC(d.u[b], ndp);
+        ALLOC(d.v[b], ndp);
+        ALLOC(d.a[b], ndp);
     }
     ALLOC(d.ctl, sizeof(Ctl));
     ALLOC(d.partials, sizeof(double2) * (size_t)npart);
     ALLOC(d.i_n, sizeof(int64_t) * (size_t)N);
+    ALLOC(d.cta_pending, sizeof(int32_t) * (size_t)nsteps_cta);
+    ALLOC(d.regen_list, sizeof(int32_t) * (size_t)N);
+    ALLOC(d.ring, sizeof(double) * (size_t)RING_MIN);
+    h->ring_cap = RING_MIN;
     if (h->is2d) {
         ALLOC(d.sq2, sizeof(double2) * (size_t)N);
     }
@@ -850,10 +851,11 @@ extern "C" int fqsb_create(const fqsb_config* cfg, fqsb_system** out)
 #undef ALLOC
     /* initSystem detail.h:1096-1139: zeros, disorder, refresh */
     cudaStream_t st = h->stream;
-    bool ok = cudaMemsetAsync(d.ctl, 0, sizeof(Ctl), st) == cudaSuccess;
+    bool ok = cudaMemsetAsync(d.ctl, 0, sizeof(Ctl), st) == cudaSuccess &&
+              cudaMemsetAsync(d.cta_pending, 0, sizeof(int32_t) * (size_t)nsteps_cta, st) == cudaSuccess;
     for (int b = 0; b < 2 && ok; ++b) {
-        ok = cudaMemsetAsync(d.u[b], 0, nd, st) == cudaSuccess && cudaMemsetAsync(d.v[b], 0, nd, st) == cudaSuccess &&
-             cudaMemsetAsync(d.a[b], 0, nd, st) == cudaSuccess;
+        ok = cudaMemsetAsync(d.u[b], 0, ndp, st) == cudaSuccess && cudaMemsetAsync(d.v[b], 0, ndp, st) == cudaSuccess &&
+             cudaMemsetAsync(d.a[b], 0, ndp, st) == cudaSuccess;
     }
     if (!ok) {
         free_all(h);

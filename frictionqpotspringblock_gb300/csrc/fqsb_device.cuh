@@ -73,6 +73,13 @@ struct Ctl {
     int32_t done;
     int32_t error;
     uint32_t ticket;
+    uint32_t ticket_redo;
+    int32_t n_pending_cta; /* CTAs of this step with a particle whose chunk window must move */
+    int32_t n_regen;       /* particles of this step whose chunk window must move */
+    int32_t pad2;
+    int64_t launch_steps;  /* steps done in the current graph launch */
+    uint64_t launch_t0;    /* %globaltimer at the first step of the current graph launch */
+    uint64_t budget_ns;    /* device time after which a graph launch yields back to the host */
     int64_t step;
     int64_t inc;
     double u_frame;
@@ -89,10 +96,20 @@ struct Ctl {
     double last_residual;
 };
 
+/* How a multiplication by a positive parameter c is carried out (all exact-equivalent to x * c). */
+enum : int { SCALE_ONE = 0, SCALE_POW2 = 1, SCALE_GENERAL = 2 };
+
+struct Scale {
+    int mode; /* SCALE_* */
+    int e;    /* c = 2^e when mode == SCALE_POW2 */
+    double c;
+};
+
 struct DevSys {
     int64_t N, rows, cols;
     int pot, inter;
     double dt, hdt, hdt2, mu, kappa, k, k_frame, me, inv_m, m;
+    Scale s_mu, s_k, s_kf, s_im; /* mu, k_interactions, k_frame, 1/m */
     /* chunk */
     int64_t W, n0;
     int dist, npar;
@@ -122,6 +139,10 @@ struct DevSys {
     int64_t* i_n;
     double2* sq2;
     int64_t npartials;
+    int32_t* cta_pending; /* per CTA of the step grid */
+    int32_t* regen_list;  /* particles whose chunk window must move (capacity N) */
+    unsigned long long h_while; /* cudaGraphConditionalHandle of the run loop */
+    unsigned long long h_if;    /* cudaGraphConditionalHandle of the regeneration branch */
 };
 
 /* ------------------------------------------------------------ pcg32 */
@@ -516,13 +537,64 @@ static __device__ __noinline__ bool dev_align(const DevSys& s, int64_t p, double
     return true;
 }
 
+/* ------------------------------------------- exact integer-pipe helpers */
+
+/* Order-preserving integer key of a double: key(a) < key(b) <=> a < b for all non-NaN a, b, with
+ * key(-0) == key(+0).  Positive NaNs sort above +inf and negative NaNs below -inf, so a NaN position
+ * never passes the well test (as the fp64 comparison). */
+__device__ __forceinline__ long long dkey(double x)
+{
+    long long b = __double_as_longlong(x);
+    long long sgn = b >> 63;
+    return (b ^ (sgn & 0x7fffffffffffffffLL)) - sgn;
+}
+
+/* yl <= u < yr, evaluated on the integer pipe (identical result to the fp64 comparisons). */
+__device__ __forceinline__ bool in_well(double yl, double yr, double u)
+{
+    long long k = dkey(u);
+    return dkey(yl) <= k && k < dkey(yr);
+}
+
+__device__ __forceinline__ bool is_nan_bits(double x)
+{
+    return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+}
+
+/* x * 2^e for a positive power of two: an exponent add when the result stays a normal number, exact
+ * like the fp64 multiplication; zeros pass through; other cases use the fp64 multiply. */
+__device__ __forceinline__ double scale_pow2(double x, int e, double c)
+{
+    long long b = __double_as_longlong(x);
+    int ex = (int)((b >> 52) & 0x7ff);
+    int ne = ex + e;
+    if (ex != 0 && ex != 0x7ff && ne >= 1 && ne <= 0x7fe) {
+        return __longlong_as_double(b + ((long long)e << 52));
+    }
+    if ((b & 0x7fffffffffffffffLL) == 0) {
+        return x;
+    }
+    return FQ_MUL(x, c);
+}
+
+/* x * c with c described by sc (c > 0 for the power-of-two forms). */
+__device__ __forceinline__ double scale(double x, const Scale& sc)
+{
+    if (sc.mode == SCALE_ONE) {
+        return x;
+    }
+    if (sc.mode == SCALE_POW2) {
+        return scale_pow2(x, sc.e, sc.c);
+    }
+    return FQ_MUL(x, sc.c);
+}
+
 /* Potential force, Cuspy detail.h:139-170 / SemiSmooth :236-277 / Smooth :379-409. */
-template <int POT, bool UNIT_MU>
+template <int POT>
 __device__ __forceinline__ double pot_force(const DevSys& s, const double4_32a& w, double up)
 {
     if (POT == POT_CUSPY) {
-        double f = FQ_SUB(w.z, up);
-        return UNIT_MU ? f : FQ_MUL(f, s.mu);
+        return scale(FQ_SUB(w.z, up), s.s_mu);
     }
     else if (POT == POT_SEMISMOOTH) {
         if (up < w.z) {

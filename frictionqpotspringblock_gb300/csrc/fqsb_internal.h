@@ -20,14 +20,15 @@ struct LineGeom {
 
 LineGeom line_geometry(int64_t N);
 
-/* One velocity-Verlet step of a Line1d / Particles system (finalises the step itself). */
-cudaError_t launch_step_line(const DevSys& s, const LineGeom& g, bool units, cudaStream_t st);
-
-/* One step of a Line2d system: step kernel + reduction/finalise kernel. */
-cudaError_t launch_step_grid(const DevSys& s, bool units, cudaStream_t st);
-
 /* Per-particle canonical reduction of the step's residual terms (used by the 2d path). */
 int64_t grid_reduce_ctas(int64_t N);
+
+/* Number of CTAs of the step kernel (size of DevSys::cta_pending and DevSys::partials). */
+int64_t step_ctas(const DevSys& s, const LineGeom& g);
+
+/* The run graph: a device-side WHILE loop over fused steps, with the chunk-regeneration branch.
+ * Writes the conditional handles into s (they are kernel arguments of the graph's nodes). */
+cudaError_t build_run_graph(DevSys& s, const LineGeom& g, cudaGraphExec_t* exec);
 
 } // namespace fqsb
 

@@ -1,27 +1,40 @@
 /*
- * Fused velocity-Verlet step kernels (sm_103a, FP64).
+ * Fused velocity-Verlet step kernels (sm_103a, FP64) and the device-side run loop.
  *
- * One launch = one System::timeStep (include/FrictionQPotSpringBlock/detail.h:1539-1570)
- * over all particles, fused with everything timeStep calls:
- *   u update (:1549), updated_u -> potential force with the well search
- *   (Cuspy::force :139-170 / SemiSmooth :236-277 / Smooth :379-409), interaction
- *   (Laplace1d::force :474-487 / Laplace2d::force :545-583), frame force (:1353-1356),
- *   three velocity updates with damping and force sums (:1552-1565, :1321-1395),
- *   the NaN check (:1567-1569),
- * and, when the run asks for it, with the residual terms of minimise / timeStepsUntilEvent
- * (residual :1512-1520, StopList test :1780-1783) and the plastic-activity bookkeeping
- * (:1768-1778, :1855-1866).  The last CTA to finish a step evaluates the step's stop tests on
- * the device, so a multi-step run needs no host synchronisation per step.
+ * One launch of k_step_line / k_step_grid = one System::timeStep
+ * (include/FrictionQPotSpringBlock/detail.h:1539-1570) over all particles, fused with everything
+ * timeStep calls: the u update (:1549), updated_u -> potential force with the well search
+ * (Cuspy::force :139-170 / SemiSmooth :236-277 / Smooth :379-409), the interaction
+ * (Laplace1d::force :474-487 / Laplace2d::force :545-583), the frame force (:1353-1356), the three
+ * velocity updates with damping and force sums (:1552-1565, :1321-1395) and the NaN check
+ * (:1567-1569); when the run asks for it also the residual terms of minimise /
+ * timeStepsUntilEvent (residual :1512-1520, StopList test :1780-1783) and the plastic-activity
+ * bookkeeping (:1768-1778, :1855-1866).
  *
- * State is double buffered (u, v, a)[cur] -> (u, v, a)[cur ^ 1]; neighbours' updated positions
- * come from shared memory inside a CTA and are recomputed from the old state at CTA edges.
- * Only a particle that leaves its current well touches its chunk row (dev_align).
+ * Run loop.  A run (timeSteps, flowSteps, minimise, minimise_truncate, timeStepsUntilEvent) is one
+ * CUDA graph: a conditional WHILE node whose body is one step.  The last CTA to finish a step
+ * evaluates the stop tests and sets the loop condition (cudaGraphSetConditional), so the host
+ * launches the graph once and synchronises once.  A launch also yields after a device-time budget
+ * (%globaltimer), so the host regains control every ~0.2 s of a long run.
  *
- * Arithmetic uses explicit __dadd_rn / __dmul_rn in the reference's order (no fma contraction),
- * so results equal the CPU oracle bit for bit.  Algebraically neutral shortcuts only:
- * the partial sum f_frame + f_potential + f_interactions is formed once per step (it is the same
- * in every computeForce of the step), and multiplications by parameters that are exactly 1.0
- * are skipped (x * 1.0 == x) in the UNITS instantiation.
+ * Chunk windows.  The step kernels only search a particle's current chunk window (a few loads).
+ * When the new well lies outside the window's margins the window must move and be regenerated from
+ * the particle's pcg32 stream (heavy code: distribution transforms).  That code is kept out of the
+ * step kernels (it would raise them to 128 registers and cost ~12% throughput); instead the CTA is
+ * marked pending, a conditional IF branch of the same graph iteration regenerates the marked
+ * particles' windows (k_regen) and re-runs the marked CTAs (redo pass).  The step is a pure function
+ * of the old state, so the redo reproduces exactly the reference's step.
+ *
+ * State is double buffered (u, v, a)[cur] -> (u, v, a)[cur ^ 1].  Arithmetic uses explicit
+ * __dadd_rn / __dmul_rn in the reference's order (no fma contraction), so results equal the CPU
+ * oracle bit for bit.  Only exact rewrites save fp64 issue slots (the fp64 pipe, ~1.6 instructions
+ * per clock per SM on GB300, is the binding unit):
+ *   - the partial sum f_frame + f_potential + f_interactions is formed once per step (it is the
+ *     same in every computeForce of the step);
+ *   - multiplications by parameters equal to 1 are skipped, and multiplications by powers of two
+ *     (2 u, 4 u, and e.g. k_frame = 2^-22) are exponent adds on the integer pipe when the result
+ *     stays normal;
+ *   - the well test yl <= u < yr and the NaN test run on order-preserving integer keys.
  */
 #include "fqsb_internal.h"
 
@@ -34,19 +47,27 @@ __device__ __forceinline__ double u_next(const DevSys& s, const double* u0, cons
 }
 
 /* velocity / acceleration updates of timeStep after the positions, detail.h:1552-1565 */
-template <bool UNITS>
 __device__ __forceinline__ void verlet_velocity(const DevSys& s, double sfi, double v0, double a0, double& v, double& a,
                                                 double& f)
 {
     v = FQ_ADD(v0, FQ_MUL(s.dt, a0));
     f = FQ_ADD(sfi, FQ_MUL(s.me, v));
-    a = UNITS ? f : FQ_MUL(f, s.inv_m);
+    a = scale(f, s.s_im);
 #pragma unroll
     for (int rep = 0; rep < 2; ++rep) {
         v = FQ_ADD(v0, FQ_MUL(s.hdt, FQ_ADD(a0, a)));
         f = FQ_ADD(sfi, FQ_MUL(s.me, v));
-        a = UNITS ? f : FQ_MUL(f, s.inv_m);
+        a = scale(f, s.s_im);
     }
+}
+
+/* (f_frame + f_potential) of the force sum, and f_frame itself */
+template <int POT>
+__device__ __forceinline__ double frame_pot(const DevSys& s, const double4_32a& w, double up, double uf, double& ff)
+{
+    double fp = pot_force<POT>(s, w, up);
+    ff = scale(FQ_SUB(uf, up), s.s_kf);
+    return FQ_ADD(ff, fp);
 }
 
 __device__ __forceinline__ long long absll(long long x)
@@ -54,93 +75,114 @@ __device__ __forceinline__ long long absll(long long x)
     return x < 0 ? -x : x;
 }
 
-/* Stop tests of one finished step; thread 0 of the last CTA.  sf / sff: sum f^2 and f_frame^2. */
+__device__ __forceinline__ uint64_t globaltimer()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void set_loop(const DevSys& s, unsigned v)
+{
+    cudaGraphSetConditional((cudaGraphConditionalHandle)s.h_while, v);
+}
+
+/*
+ * Stop tests of one finished step (thread 0 of the CTA that finishes the step last); sets the
+ * run-loop condition.  sf / sff: sum of f^2 and of f_frame^2 over all particles.
+ */
 __device__ void finalize_step(const DevSys& s, double uf, double sf, double sff)
 {
     Ctl* c = s.ctl;
     int flags = c->flags;
     c->ticket = 0;
+    c->ticket_redo = 0;
+    c->n_pending_cta = 0;
+    c->n_regen = 0;
     c->step += 1;
     c->inc += 1;
     c->cur ^= 1;
     if (flags & RF_FLOW) {
         c->u_frame = uf;
     }
+    uint64_t now = globaltimer();
+    if (c->launch_steps == 0) {
+        c->launch_t0 = now;
+    }
+    c->launch_steps += 1;
     if (c->nan_flag) {
         c->error = DERR_NAN;
-        return;
     }
-    if (c->walk_flag) {
+    else if (c->walk_flag) {
         c->error = DERR_WALK;
-        return;
     }
-    if (flags & (RF_ACT | RF_TRUNCATE)) {
-        long long sv = c->s_sum;
-        if (sv != c->s_n) {
-            if (c->init) {
-                c->init = 0;
-                c->qs_first = c->inc;
+    else {
+        if (flags & (RF_ACT | RF_TRUNCATE)) {
+            long long sv = c->s_sum;
+            if (sv != c->s_n) {
+                if (c->init) {
+                    c->init = 0;
+                    c->qs_first = c->inc;
+                }
+                c->qs_last = c->inc;
             }
-            c->qs_last = c->inc;
+            c->s_n = sv;
         }
-        c->s_n = sv;
-    }
-    if (flags & RF_EVENT) {
-        if (c->a_count != 0) {
+        if ((flags & RF_EVENT) && c->a_count != 0) {
             c->done = RUN_EVENT;
-            return;
         }
-    }
-    if (flags & RF_RESID) {
-        double r_fres = FQ_SQRT(sf);
-        double r_fext = FQ_SQRT(sff);
-        double r = r_fext != 0.0 ? FQ_DIV(r_fres, r_fext) : r_fres;
-        c->last_residual = r;
-        int64_t n = c->niter_tol;
-        if (n > 0) {
-            double* ring = s.ring;
-            int64_t pos = c->sl_pos;
-            double old = ring[pos];
-            if (old >= c->tol) {
-                c->sl_ge_tol -= 1;
-            }
-            if (old >= c->tol2) {
-                c->sl_ge_tol2 -= 1;
-            }
-            if (n >= 2) {
-                double second = ring[(pos + 1) % n];
-                if (second > old) {
-                    c->sl_asc -= 1;
+        if (!c->done && (flags & RF_RESID)) {
+            double r_fres = FQ_SQRT(sf);
+            double r_fext = FQ_SQRT(sff);
+            double r = r_fext != 0.0 ? FQ_DIV(r_fres, r_fext) : r_fres;
+            c->last_residual = r;
+            int64_t n = c->niter_tol;
+            if (n > 0) {
+                double* ring = s.ring;
+                int64_t pos = c->sl_pos;
+                double old = ring[pos];
+                if (old >= c->tol) {
+                    c->sl_ge_tol -= 1;
                 }
-                double newest = ring[(pos + n - 1) % n];
-                if (r > newest) {
-                    c->sl_asc += 1;
+                if (old >= c->tol2) {
+                    c->sl_ge_tol2 -= 1;
+                }
+                if (n >= 2) {
+                    double second = ring[(pos + 1) % n];
+                    if (second > old) {
+                        c->sl_asc -= 1;
+                    }
+                    double newest = ring[(pos + n - 1) % n];
+                    if (r > newest) {
+                        c->sl_asc += 1;
+                    }
+                }
+                ring[pos] = r;
+                c->sl_pos = (pos + 1) % n;
+                if (r >= c->tol) {
+                    c->sl_ge_tol += 1;
+                }
+                if (r >= c->tol2) {
+                    c->sl_ge_tol2 += 1;
                 }
             }
-            ring[pos] = r;
-            c->sl_pos = (pos + 1) % n;
-            if (r >= c->tol) {
-                c->sl_ge_tol += 1;
-            }
-            if (r >= c->tol2) {
-                c->sl_ge_tol2 += 1;
+            if ((c->sl_asc == 0 && c->sl_ge_tol == 0) || c->sl_ge_tol2 == 0) {
+                c->done = RUN_CONVERGED;
             }
         }
-        if ((c->sl_asc == 0 && c->sl_ge_tol == 0) || c->sl_ge_tol2 == 0) {
-            c->done = RUN_CONVERGED;
-            return;
+        if (!c->done && (flags & RF_TRUNCATE)) {
+            if ((c->A_truncate > 0 && c->a_count >= c->A_truncate) ||
+                (c->S_truncate > 0 && c->s_sum >= c->S_truncate)) {
+                c->done = RUN_TRUNCATED;
+            }
+        }
+        if (!c->done && c->step >= c->max_steps) {
+            c->done = RUN_MAXITER;
         }
     }
-    if (flags & RF_TRUNCATE) {
-        if ((c->A_truncate > 0 && c->a_count >= c->A_truncate) ||
-            (c->S_truncate > 0 && c->s_sum >= c->S_truncate)) {
-            c->done = RUN_TRUNCATED;
-            return;
-        }
-    }
-    if (c->step >= c->max_steps) {
-        c->done = RUN_MAXITER;
-    }
+    bool more = !c->done && !c->error && (now - c->launch_t0) < c->budget_ns;
+    __threadfence();
+    set_loop(s, more ? 1u : 0u);
 }
 
 /* Whole-CTA canonical tree over partials[0..G) (zero padded to a power of two). */
@@ -174,15 +216,18 @@ struct StepShared {
     int flags;
     int last;
     int nan;
+    int pending;
     double uf;
     unsigned long long ds;
     unsigned long long da;
     double red[32];
 };
 
-__device__ __forceinline__ bool step_prologue(const DevSys& s, StepShared& sh)
+/* Reads the run state; returns false when the run is already over (then CTA 0 ends the loop). */
+__device__ __forceinline__ bool step_prologue(const DevSys& s, StepShared& sh, bool graph_loop)
 {
-    if (threadIdx.x == 0 && threadIdx.y == 0) {
+    int tid = threadIdx.x + threadIdx.y * blockDim.x;
+    if (tid == 0) {
         volatile Ctl* c = s.ctl;
         sh.exit_flag = (c->done != 0) || (c->error != 0);
         sh.cur = c->cur;
@@ -193,22 +238,68 @@ __device__ __forceinline__ bool step_prologue(const DevSys& s, StepShared& sh)
         }
         sh.uf = uf;
         sh.nan = 0;
+        sh.pending = 0;
         sh.ds = 0ull;
         sh.da = 0ull;
         sh.last = 0;
+        if (sh.exit_flag && graph_loop && blockIdx.x == 0 && blockIdx.y == 0) {
+            set_loop(s, 0u);
+        }
     }
     __syncthreads();
     return sh.exit_flag == 0;
 }
 
-/* Per-particle well check + bookkeeping; returns the (possibly refreshed) well cache. */
-__device__ __forceinline__ double4_32a well_of(const DevSys& s, int64_t p, double un, bool act, StepShared& sh)
+/*
+ * Searches particle p's current chunk window for the well of u (y[i] <= u < y[i+1], the prrng
+ * align rule) and commits it when it lies inside the window's margins [min_margin, W - buffer).
+ * Returns false when the window must move (then nothing is changed).
+ */
+__device__ __forceinline__ bool window_search(const DevSys& s, int64_t p, double u, double4_32a& w)
+{
+    const int64_t W = s.W;
+    const double* y = s.data + p * W;
+    if (!(y[0] <= u && u < y[W - 1])) {
+        return false;
+    }
+    int64_t li = s.cidx[p];
+    if (y[li] <= u) {
+        while (li + 1 < W && y[li + 1] <= u) {
+            ++li;
+        }
+    }
+    else {
+        while (li > 0 && y[li] > u) {
+            --li;
+        }
+    }
+    if (li < s.min_margin || li >= W - s.buffer) {
+        return false;
+    }
+    s.cidx[p] = (int32_t)li;
+    s.gidx[p] = s.start[p] + li;
+    w = make_wc(s, y[li], y[li + 1]);
+    s.wc[p] = w;
+    return true;
+}
+
+__device__ __forceinline__ bool non_finite(double x)
+{
+    return (__double_as_longlong(x) & 0x7fffffffffffffffLL) >= 0x7ff0000000000000LL;
+}
+
+/*
+ * Per-particle well check; returns the (possibly refreshed) well cache.  `regen` is set when the
+ * particle's chunk window must move; the pass-1 caller then marks its CTA pending.
+ */
+__device__ __forceinline__ double4_32a well_of(const DevSys& s, int64_t p, double un, bool act, StepShared& sh,
+                                               bool& regen)
 {
     double4_32a w = s.wc[p];
-    if (!(w.x <= un && un < w.y)) {
+    regen = false;
+    if (!in_well(w.x, w.y, un) && !non_finite(un)) {
         int64_t gold = s.gidx[p];
-        if (dev_align(s, p, un)) {
-            w = s.wc[p];
+        if (window_search(s, p, un, w)) {
             int64_t gnew = s.gidx[p];
             if (act && gnew != gold) {
                 int64_t ref = s.i_n[p];
@@ -218,16 +309,31 @@ __device__ __forceinline__ double4_32a well_of(const DevSys& s, int64_t p, doubl
                 atomicAdd(&sh.da, (unsigned long long)da);
             }
         }
+        else {
+            regen = true;
+        }
     }
     return w;
 }
 
-__device__ __forceinline__ void step_epilogue(const DevSys& s, StepShared& sh, bool finalize_here, double rf,
-                                              double rff)
+/* Role of the CTA epilogue in the step's kernels. */
+enum : int {
+    EPI_LINE = 0,      /* 1d pass 1: last CTA finalises, or opens the regeneration branch */
+    EPI_GRID_STEP = 1, /* 2d pass 1: last CTA opens (or closes) the regeneration branch */
+    EPI_REDO = 2,      /* 1d redo of the pending CTAs: the last of them finalises */
+    EPI_REDUCE = 3     /* 2d reduction: last CTA finalises */
+};
+
+/*
+ * End of a CTA's part of a step: commits activity / NaN flags and the CTA's residual subtree; the CTA
+ * that finishes last (ticket) finalises the step or steers the regeneration branch, per `mode`.
+ */
+__device__ __forceinline__ void step_epilogue(const DevSys& s, StepShared& sh, int mode, double rf, double rff)
 {
-    bool resid = (sh.flags & RF_RESID) != 0;
+    const bool resid = (sh.flags & RF_RESID) != 0;
+    const bool tree = resid && mode != EPI_GRID_STEP;
     double sf = 0.0, sff = 0.0;
-    if (resid && finalize_here) {
+    if (tree) {
         sf = cta_tree(rf, sh.red);
         __syncthreads();
         sff = cta_tree(rff, sh.red);
@@ -235,9 +341,9 @@ __device__ __forceinline__ void step_epilogue(const DevSys& s, StepShared& sh, b
     __syncthreads();
     int tid = threadIdx.x + threadIdx.y * blockDim.x;
     int64_t bid = blockIdx.x + (int64_t)blockIdx.y * gridDim.x;
+    Ctl* c = s.ctl;
     if (tid == 0) {
-        Ctl* c = s.ctl;
-        if (resid && finalize_here) {
+        if (tree) {
             s.partials[bid] = make_double2(sf, sff);
         }
         if (sh.ds) {
@@ -246,43 +352,74 @@ __device__ __forceinline__ void step_epilogue(const DevSys& s, StepShared& sh, b
         if (sh.da) {
             atomicAdd((unsigned long long*)&c->a_count, sh.da);
         }
-        if (sh.nan) {
+        if (sh.nan && !sh.pending) {
             atomicOr(&c->nan_flag, 1);
         }
-        if (finalize_here) {
-            __threadfence();
-            unsigned int t = atomicAdd(&c->ticket, 1u);
-            sh.last = (t == gridDim.x * gridDim.y - 1);
+        if (sh.pending) {
+            s.cta_pending[bid] = 1;
+            atomicAdd(&c->n_pending_cta, 1);
         }
-    }
-    if (!finalize_here) {
-        return;
+        __threadfence();
+        if (mode == EPI_REDO) {
+            unsigned t = atomicAdd(&c->ticket_redo, 1u);
+            sh.last = (t == (unsigned)c->n_pending_cta - 1u) ? 1 : 0;
+        }
+        else {
+            unsigned t = atomicAdd(&c->ticket, 1u);
+            sh.last = (t == gridDim.x * gridDim.y - 1) ? 1 : 0;
+        }
     }
     __syncthreads();
-    if (sh.last) {
-        __threadfence();
-        double2 tot = make_double2(0.0, 0.0);
-        if (resid) {
-            tot = tree_partials(s.partials, (int64_t)gridDim.x * gridDim.y, sh.red);
+    if (!sh.last) {
+        return;
+    }
+    __threadfence();
+    if (mode == EPI_LINE || mode == EPI_GRID_STEP) {
+        bool pend = c->n_pending_cta > 0;
+        if (pend || mode == EPI_GRID_STEP) {
+            if (tid == 0) {
+                c->ticket = 0;
+                cudaGraphSetConditional((cudaGraphConditionalHandle)s.h_if, pend ? 1u : 0u);
+            }
+            return;
         }
         if (tid == 0) {
-            finalize_step(s, sh.uf, tot.x, tot.y);
+            cudaGraphSetConditional((cudaGraphConditionalHandle)s.h_if, 0u);
         }
+    }
+    double2 tot = make_double2(0.0, 0.0);
+    if (resid) {
+        tot = tree_partials(s.partials, (int64_t)gridDim.x * gridDim.y, sh.red);
+    }
+    if (tid == 0) {
+        finalize_step(s, sh.uf, tot.x, tot.y);
     }
 }
 
 /*
- * Line1d (INTER_LAPLACE1D) or Particles (INTER_NONE) step.  Thread t of CTA b owns particles
- * b*T*PPT + t*PPT + [0, PPT): a CTA covers an aligned power-of-two range of the flat index, so the
- * residual sums follow the fixed pairwise tree over the flat index.
+ * Line1d (INTER_LAPLACE1D) or Particles (INTER_NONE) step.  Thread t of CTA b owns the PPT consecutive
+ * particles b*T*PPT + t*PPT + [0, PPT): a CTA covers an aligned power-of-two range of the flat index,
+ * so the residual sums follow the fixed pairwise tree over the flat index.  Updated positions are
+ * exchanged through shared memory (one barrier); the two particles just outside the CTA are recomputed
+ * from the old state.  State arrays are padded to a multiple of 1024 entries.  redo = 1: only CTAs
+ * marked pending run (after k_regen moved their particles' windows).
  */
-template <int POT, int INTER, bool UNITS, int PPT>
-__global__ void __launch_bounds__(256) k_step_line(DevSys s)
+template <int POT, int INTER, int PPT>
+__global__ void __launch_bounds__(256) k_step_line(DevSys s, int redo)
 {
     __shared__ StepShared sh;
     __shared__ double sh_un[256 * PPT];
-    if (!step_prologue(s, sh)) {
+    if (!step_prologue(s, sh, true)) {
         return;
+    }
+    if (redo) {
+        if (!s.cta_pending[blockIdx.x]) {
+            return;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            s.cta_pending[blockIdx.x] = 0;
+        }
     }
     const int cur = sh.cur;
     const bool act = (sh.flags & (RF_ACT | RF_TRUNCATE | RF_EVENT)) != 0;
@@ -291,6 +428,7 @@ __global__ void __launch_bounds__(256) k_step_line(DevSys s)
     const int64_t N = s.N;
     const int T = blockDim.x;
     const int64_t base = (int64_t)blockIdx.x * T * PPT;
+    const int64_t p0 = base + (int64_t)threadIdx.x * PPT;
     const double* u0 = s.u[cur];
     const double* v0 = s.v[cur];
     const double* a0 = s.a[cur];
@@ -299,64 +437,63 @@ __global__ void __launch_bounds__(256) k_step_line(DevSys s)
     double* a1 = s.a[cur ^ 1];
 
     double un[PPT], vr[PPT], ar[PPT];
+    if (PPT == 2) {
+        double2 uu = *reinterpret_cast<const double2*>(u0 + p0);
+        double2 vv = *reinterpret_cast<const double2*>(v0 + p0);
+        double2 aa = *reinterpret_cast<const double2*>(a0 + p0);
+        vr[0] = vv.x;
+        vr[PPT - 1] = vv.y;
+        ar[0] = aa.x;
+        ar[PPT - 1] = aa.y;
+        un[0] = FQ_ADD(FQ_ADD(uu.x, FQ_MUL(s.dt, vr[0])), FQ_MUL(s.hdt2, ar[0]));
+        un[PPT - 1] = FQ_ADD(FQ_ADD(uu.y, FQ_MUL(s.dt, vr[PPT - 1])), FQ_MUL(s.hdt2, ar[PPT - 1]));
+    }
+    else {
 #pragma unroll
-    for (int j = 0; j < PPT; ++j) {
-        int64_t p = base + threadIdx.x * PPT + j;
-        if (p < N) {
-            vr[j] = v0[p];
-            ar[j] = a0[p];
-            un[j] = FQ_ADD(FQ_ADD(u0[p], FQ_MUL(s.dt, vr[j])), FQ_MUL(s.hdt2, ar[j]));
-            if (INTER == INTER_LAPLACE1D) {
-                sh_un[threadIdx.x * PPT + j] = un[j];
-            }
+        for (int j = 0; j < PPT; ++j) {
+            vr[j] = v0[p0 + j];
+            ar[j] = a0[p0 + j];
+            un[j] = FQ_ADD(FQ_ADD(u0[p0 + j], FQ_MUL(s.dt, vr[j])), FQ_MUL(s.hdt2, ar[j]));
         }
     }
     if (INTER == INTER_LAPLACE1D) {
+#pragma unroll
+        for (int j = 0; j < PPT; ++j) {
+            sh_un[threadIdx.x * PPT + j] = un[j];
+        }
         __syncthreads();
     }
     double rf = 0.0, rff = 0.0;
-    bool nan = false;
+    bool nan = false, pending = false;
+    double vo[PPT], ao[PPT];
 #pragma unroll
     for (int j = 0; j < PPT; ++j) {
-        int64_t p = base + threadIdx.x * PPT + j;
+        int64_t p = p0 + j;
+        vo[j] = 0.0;
+        ao[j] = 0.0;
         if (p >= N) {
             continue;
         }
         double up = un[j];
-        double4_32a w = well_of(s, p, up, act, sh);
-        double fp = pot_force<POT, UNITS>(s, w, up);
+        bool regen;
+        double4_32a w = well_of(s, p, up, act, sh, regen);
+        pending |= regen;
+        double ff;
+        double sfp = frame_pot<POT>(s, w, up, uf, ff);
         double fi = 0.0;
         if (INTER == INTER_LAPLACE1D) {
             int li = threadIdx.x * PPT + j;
-            double uL, uR;
-            if (li > 0) {
-                uL = sh_un[li - 1];
-            }
-            else {
-                uL = u_next(s, u0, v0, a0, p == 0 ? N - 1 : p - 1);
-            }
-            if (li + 1 < T * PPT && p + 1 < N) {
-                uR = sh_un[li + 1];
-            }
-            else {
-                uR = u_next(s, u0, v0, a0, p == N - 1 ? 0 : p + 1);
-            }
-            fi = FQ_ADD(FQ_SUB(uL, FQ_MUL(2.0, up)), uR);
-            if (!UNITS) {
-                fi = FQ_MUL(fi, s.k);
-            }
+            double uL = li > 0 ? sh_un[li - 1] : u_next(s, u0, v0, a0, p == 0 ? N - 1 : p - 1);
+            double uR = (li + 1 < T * PPT && p + 1 < N) ? sh_un[li + 1] : u_next(s, u0, v0, a0, p + 1 == N ? 0 : p + 1);
+            fi = scale(FQ_ADD(FQ_SUB(uL, scale_pow2(up, 1, 2.0)), uR), s.s_k);
         }
-        double ff = FQ_MUL(s.k_frame, FQ_SUB(uf, up));
-        double sfi = FQ_ADD(FQ_ADD(ff, fp), fi);
-        double vv, aa, f;
-        verlet_velocity<UNITS>(s, sfi, vr[j], ar[j], vv, aa, f);
-        u1[p] = up;
-        v1[p] = vv;
-        a1[p] = aa;
-        nan |= (up != up);
+        double sfi = FQ_ADD(sfp, fi);
+        double f;
+        verlet_velocity(s, sfi, vr[j], ar[j], vo[j], ao[j], f);
+        nan |= is_nan_bits(up);
         if (resid) {
             double f2 = FQ_MUL(f, f), ff2 = FQ_MUL(ff, ff);
-            if (PPT == 1 || j == 0) {
+            if (j == 0) {
                 rf = f2;
                 rff = ff2;
             }
@@ -366,10 +503,43 @@ __global__ void __launch_bounds__(256) k_step_line(DevSys s)
             }
         }
     }
+    if (p0 < N) {
+        if (PPT == 2) {
+            *reinterpret_cast<double2*>(u1 + p0) = make_double2(un[0], un[PPT - 1]);
+            *reinterpret_cast<double2*>(v1 + p0) = make_double2(vo[0], vo[PPT - 1]);
+            *reinterpret_cast<double2*>(a1 + p0) = make_double2(ao[0], ao[PPT - 1]);
+        }
+        else {
+#pragma unroll
+            for (int j = 0; j < PPT; ++j) {
+                u1[p0 + j] = un[j];
+                v1[p0 + j] = vo[j];
+                a1[p0 + j] = ao[j];
+            }
+        }
+    }
     if (nan) {
         sh.nan = 1;
     }
-    step_epilogue(s, sh, true, rf, rff);
+    if (pending && !redo) {
+        sh.pending = 1;
+        for (int j = 0; j < PPT; ++j) {
+            /* record the particles of this thread that need a new window */
+            int64_t p = p0 + j;
+            if (p < N) {
+                double4_32a w = s.wc[p];
+                if (!in_well(w.x, w.y, un[j]) && !non_finite(un[j])) {
+                    int k = atomicAdd(&s.ctl->n_regen, 1);
+                    s.regen_list[k] = (int32_t)p;
+                }
+            }
+        }
+    }
+    if (pending && redo) {
+        /* the window could not be moved (yield search bound): reported by the finalisation */
+        atomicOr(&s.ctl->walk_flag, 1);
+    }
+    step_epilogue(s, sh, redo ? EPI_REDO : EPI_LINE, rf, rff);
 }
 
 /*
@@ -377,13 +547,23 @@ __global__ void __launch_bounds__(256) k_step_line(DevSys s)
  * written per particle (sq2) and summed in the flat-index pairwise order by k_reduce_grid, which
  * also finalises the step.
  */
-template <int POT, bool UNITS>
-__global__ void __launch_bounds__(256) k_step_grid(DevSys s)
+template <int POT>
+__global__ void __launch_bounds__(256) k_step_grid(DevSys s, int redo)
 {
     __shared__ StepShared sh;
     __shared__ double sh_un[8][32];
-    if (!step_prologue(s, sh)) {
+    if (!step_prologue(s, sh, true)) {
         return;
+    }
+    const int64_t bid = blockIdx.x + (int64_t)blockIdx.y * gridDim.x;
+    if (redo) {
+        if (!s.cta_pending[bid]) {
+            return;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0 && threadIdx.y == 0) {
+            s.cta_pending[bid] = 0;
+        }
     }
     const int cur = sh.cur;
     const bool act = (sh.flags & (RF_ACT | RF_TRUNCATE | RF_EVENT)) != 0;
@@ -407,38 +587,62 @@ __global__ void __launch_bounds__(256) k_step_grid(DevSys s)
     }
     __syncthreads();
     if (valid) {
-        double4_32a w = well_of(s, p, up, act, sh);
-        double fp = pot_force<POT, UNITS>(s, w, up);
+        bool regen;
+        double4_32a w = well_of(s, p, up, act, sh, regen);
+        if (regen) {
+            if (!redo) {
+                sh.pending = 1;
+                int k = atomicAdd(&s.ctl->n_regen, 1);
+                s.regen_list[k] = (int32_t)p;
+            }
+            else {
+                atomicOr(&s.ctl->walk_flag, 1);
+            }
+        }
+        double ff;
+        double sfp = frame_pot<POT>(s, w, up, uf, ff);
         double uU = ty > 0 ? sh_un[ty - 1][tx] : u_next(s, u0, v0, a0, ((i + R - 1) % R) * C + jc);
         double uD = (ty < 7 && i + 1 < R) ? sh_un[ty + 1][tx] : u_next(s, u0, v0, a0, ((i + 1) % R) * C + jc);
         double uL = tx > 0 ? sh_un[ty][tx - 1] : u_next(s, u0, v0, a0, i * C + (jc + C - 1) % C);
         double uR = (tx < 31 && jc + 1 < C) ? sh_un[ty][tx + 1] : u_next(s, u0, v0, a0, i * C + (jc + 1) % C);
-        double fi = FQ_SUB(FQ_ADD(FQ_ADD(FQ_ADD(uU, uD), uL), uR), FQ_MUL(4.0, up));
-        if (!UNITS) {
-            fi = FQ_MUL(fi, s.k);
-        }
-        double ff = FQ_MUL(s.k_frame, FQ_SUB(uf, up));
-        double sfi = FQ_ADD(FQ_ADD(ff, fp), fi);
+        double fi = scale(FQ_SUB(FQ_ADD(FQ_ADD(FQ_ADD(uU, uD), uL), uR), scale_pow2(up, 2, 4.0)), s.s_k);
+        double sfi = FQ_ADD(sfp, fi);
         double vv, aa, f;
-        verlet_velocity<UNITS>(s, sfi, vr, ar, vv, aa, f);
+        verlet_velocity(s, sfi, vr, ar, vv, aa, f);
         s.u[cur ^ 1][p] = up;
         s.v[cur ^ 1][p] = vv;
         s.a[cur ^ 1][p] = aa;
-        if (up != up) {
+        if (is_nan_bits(up)) {
             sh.nan = 1;
         }
         if (resid) {
             s.sq2[p] = make_double2(FQ_MUL(f, f), FQ_MUL(ff, ff));
         }
     }
-    step_epilogue(s, sh, false, 0.0, 0.0);
+    if (redo) {
+        /* the reduction kernel after the branch finalises; only the counters are committed here */
+        __syncthreads();
+        if (threadIdx.x == 0 && threadIdx.y == 0) {
+            if (sh.ds) {
+                atomicAdd((unsigned long long*)&s.ctl->s_sum, sh.ds);
+            }
+            if (sh.da) {
+                atomicAdd((unsigned long long*)&s.ctl->a_count, sh.da);
+            }
+            if (sh.nan) {
+                atomicOr(&s.ctl->nan_flag, 1);
+            }
+        }
+        return;
+    }
+    step_epilogue(s, sh, EPI_GRID_STEP, 0.0, 0.0);
 }
 
 /* Pairwise reduction of the 2d step's sq2 in flat-index order (1024 per CTA) + step finalisation. */
 __global__ void __launch_bounds__(256) k_reduce_grid(DevSys s)
 {
     __shared__ StepShared sh;
-    if (!step_prologue(s, sh)) {
+    if (!step_prologue(s, sh, true)) {
         return;
     }
     const bool resid = (sh.flags & RF_RESID) != 0;
@@ -461,10 +665,36 @@ __global__ void __launch_bounds__(256) k_reduce_grid(DevSys s)
         rf = FQ_ADD(FQ_ADD(x[0], x[1]), FQ_ADD(x[2], x[3]));
         rff = FQ_ADD(FQ_ADD(y[0], y[1]), FQ_ADD(y[2], y[3]));
     }
-    step_epilogue(s, sh, true, rf, rff);
+    step_epilogue(s, sh, EPI_REDUCE, rf, rff);
 }
 
-/* ------------------------------------------------------------- launchers */
+/* Regeneration branch: move the chunk windows of the particles recorded by pass 1. */
+__global__ void __launch_bounds__(128) k_regen(DevSys s)
+{
+    Ctl* c = s.ctl;
+    if (c->done || c->error) {
+        return;
+    }
+    const int cur = c->cur;
+    const bool act = (c->flags & (RF_ACT | RF_TRUNCATE | RF_EVENT)) != 0;
+    const int n = c->n_regen;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        int64_t p = s.regen_list[k];
+        double un = u_next(s, s.u[cur], s.v[cur], s.a[cur], p);
+        int64_t gold = s.gidx[p];
+        dev_align(s, p, un);
+        int64_t gnew = s.gidx[p];
+        if (act && gnew != gold) {
+            int64_t ref = s.i_n[p];
+            long long ds = absll(gnew - ref) - absll(gold - ref);
+            long long da = (long long)(gnew != ref) - (long long)(gold != ref);
+            atomicAdd((unsigned long long*)&c->s_sum, (unsigned long long)ds);
+            atomicAdd((unsigned long long*)&c->a_count, (unsigned long long)da);
+        }
+    }
+}
+
+/* ------------------------------------------------------------- geometry */
 
 LineGeom line_geometry(int64_t N)
 {
@@ -485,81 +715,132 @@ int64_t grid_reduce_ctas(int64_t N)
     return (N + 1023) / 1024;
 }
 
-template <int POT, int INTER>
-static cudaError_t launch_line_t(const DevSys& s, const LineGeom& g, bool units, cudaStream_t st)
+int64_t step_ctas(const DevSys& s, const LineGeom& g)
 {
-    dim3 grid((unsigned)g.grid), block((unsigned)g.threads);
-    if (g.ppt == 2) {
-        if (units) {
-            k_step_line<POT, INTER, true, 2><<<grid, block, 0, st>>>(s);
-        }
-        else {
-            k_step_line<POT, INTER, false, 2><<<grid, block, 0, st>>>(s);
-        }
+    if (s.inter == INTER_LAPLACE2D) {
+        return ((s.cols + 31) / 32) * ((s.rows + 7) / 8);
     }
-    else {
-        if (units) {
-            k_step_line<POT, INTER, true, 1><<<grid, block, 0, st>>>(s);
-        }
-        else {
-            k_step_line<POT, INTER, false, 1><<<grid, block, 0, st>>>(s);
-        }
-    }
-    return cudaGetLastError();
+    return g.grid;
 }
 
-cudaError_t launch_step_line(const DevSys& s, const LineGeom& g, bool units, cudaStream_t st)
+/* ------------------------------------------------------------- run graph */
+
+template <int POT, int INTER>
+static void* line_kernel_t(int ppt)
 {
+    return ppt == 2 ? (void*)k_step_line<POT, INTER, 2> : (void*)k_step_line<POT, INTER, 1>;
+}
+
+static void* step_kernel(const DevSys& s, const LineGeom& g)
+{
+    if (s.inter == INTER_LAPLACE2D) {
+        switch (s.pot) {
+            case POT_CUSPY: return (void*)k_step_grid<POT_CUSPY>;
+            case POT_SEMISMOOTH: return (void*)k_step_grid<POT_SEMISMOOTH>;
+            default: return (void*)k_step_grid<POT_SMOOTH>;
+        }
+    }
     if (s.inter == INTER_LAPLACE1D) {
         switch (s.pot) {
-            case POT_CUSPY: return launch_line_t<POT_CUSPY, INTER_LAPLACE1D>(s, g, units, st);
-            case POT_SEMISMOOTH: return launch_line_t<POT_SEMISMOOTH, INTER_LAPLACE1D>(s, g, units, st);
-            default: return launch_line_t<POT_SMOOTH, INTER_LAPLACE1D>(s, g, units, st);
+            case POT_CUSPY: return line_kernel_t<POT_CUSPY, INTER_LAPLACE1D>(g.ppt);
+            case POT_SEMISMOOTH: return line_kernel_t<POT_SEMISMOOTH, INTER_LAPLACE1D>(g.ppt);
+            default: return line_kernel_t<POT_SMOOTH, INTER_LAPLACE1D>(g.ppt);
         }
     }
     switch (s.pot) {
-        case POT_CUSPY: return launch_line_t<POT_CUSPY, INTER_NONE>(s, g, units, st);
-        case POT_SEMISMOOTH: return launch_line_t<POT_SEMISMOOTH, INTER_NONE>(s, g, units, st);
-        default: return launch_line_t<POT_SMOOTH, INTER_NONE>(s, g, units, st);
+        case POT_CUSPY: return line_kernel_t<POT_CUSPY, INTER_NONE>(g.ppt);
+        case POT_SEMISMOOTH: return line_kernel_t<POT_SEMISMOOTH, INTER_NONE>(g.ppt);
+        default: return line_kernel_t<POT_SMOOTH, INTER_NONE>(g.ppt);
     }
 }
 
-cudaError_t launch_step_grid(const DevSys& s, bool units, cudaStream_t st)
+static cudaError_t add_kernel(cudaGraphNode_t* node, cudaGraph_t graph, const cudaGraphNode_t* deps, size_t ndeps,
+                              void* func, dim3 grid, dim3 block, void** args)
 {
-    dim3 block(32, 8);
-    dim3 grid((unsigned)((s.cols + 31) / 32), (unsigned)((s.rows + 7) / 8));
-    switch (s.pot) {
-        case POT_CUSPY:
-            if (units) {
-                k_step_grid<POT_CUSPY, true><<<grid, block, 0, st>>>(s);
-            }
-            else {
-                k_step_grid<POT_CUSPY, false><<<grid, block, 0, st>>>(s);
-            }
-            break;
-        case POT_SEMISMOOTH:
-            if (units) {
-                k_step_grid<POT_SEMISMOOTH, true><<<grid, block, 0, st>>>(s);
-            }
-            else {
-                k_step_grid<POT_SEMISMOOTH, false><<<grid, block, 0, st>>>(s);
-            }
-            break;
-        default:
-            if (units) {
-                k_step_grid<POT_SMOOTH, true><<<grid, block, 0, st>>>(s);
-            }
-            else {
-                k_step_grid<POT_SMOOTH, false><<<grid, block, 0, st>>>(s);
-            }
-            break;
+    cudaKernelNodeParams kp = {};
+    kp.func = func;
+    kp.gridDim = grid;
+    kp.blockDim = block;
+    kp.sharedMemBytes = 0;
+    kp.kernelParams = args;
+    kp.extra = nullptr;
+    return cudaGraphAddKernelNode(node, graph, deps, ndeps, &kp);
+}
+
+static cudaError_t add_conditional(cudaGraphNode_t* node, cudaGraph_t graph, const cudaGraphNode_t* deps, size_t ndeps,
+                                   cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type, cudaGraph_t* body)
+{
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = type;
+    np.conditional.size = 1;
+    cudaError_t e = cudaGraphAddNode(node, graph, deps, nullptr, ndeps, &np);
+    if (e == cudaSuccess) {
+        *body = np.conditional.phGraph_out[0];
     }
-    cudaError_t e = cudaGetLastError();
+    return e;
+}
+
+#define GR(expr)                                                                                       \
+    do {                                                                                               \
+        cudaError_t e_ = (expr);                                                                       \
+        if (e_ != cudaSuccess) {                                                                       \
+            cudaGraphDestroy(g);                                                                       \
+            return e_;                                                                                 \
+        }                                                                                              \
+    } while (0)
+
+/*
+ * The run graph: WHILE(h_while) { step pass 1 ; IF(h_if) { regenerate windows ; redo pending CTAs } ;
+ * [2d: reduce + finalise] }.  `s` is updated with the two conditional handles (kernel arguments).
+ */
+cudaError_t build_run_graph(DevSys& s, const LineGeom& g0, cudaGraphExec_t* exec)
+{
+    cudaGraph_t g;
+    cudaError_t e = cudaGraphCreate(&g, 0);
     if (e != cudaSuccess) {
         return e;
     }
-    k_reduce_grid<<<(unsigned)grid_reduce_ctas(s.N), 256, 0, st>>>(s);
-    return cudaGetLastError();
+    cudaGraphConditionalHandle hw, hi;
+    GR(cudaGraphConditionalHandleCreate(&hw, g, 1, cudaGraphCondAssignDefault));
+    cudaGraphNode_t wnode;
+    cudaGraph_t body;
+    GR(add_conditional(&wnode, g, nullptr, 0, hw, cudaGraphCondTypeWhile, &body));
+    GR(cudaGraphConditionalHandleCreate(&hi, body, 0, cudaGraphCondAssignDefault));
+    s.h_while = hw;
+    s.h_if = hi;
+
+    bool is2d = s.inter == INTER_LAPLACE2D;
+    dim3 grid, block;
+    if (is2d) {
+        grid = dim3((unsigned)((s.cols + 31) / 32), (unsigned)((s.rows + 7) / 8));
+        block = dim3(32, 8);
+    }
+    else {
+        grid = dim3((unsigned)g0.grid);
+        block = dim3((unsigned)g0.threads);
+    }
+    void* fstep = step_kernel(s, g0);
+    int pass1 = 0, pass2 = 1;
+    void* args1[] = {(void*)&s, (void*)&pass1};
+    void* args2[] = {(void*)&s, (void*)&pass2};
+    void* argsr[] = {(void*)&s};
+    cudaGraphNode_t nstep, nif;
+    GR(add_kernel(&nstep, body, nullptr, 0, fstep, grid, block, args1));
+    cudaGraph_t ifbody;
+    GR(add_conditional(&nif, body, &nstep, 1, hi, cudaGraphCondTypeIf, &ifbody));
+    cudaGraphNode_t nregen, nredo;
+    GR(add_kernel(&nregen, ifbody, nullptr, 0, (void*)k_regen, dim3(4 * 152), dim3(128), argsr));
+    GR(add_kernel(&nredo, ifbody, &nregen, 1, fstep, grid, block, args2));
+    if (is2d) {
+        cudaGraphNode_t nred;
+        GR(add_kernel(&nred, body, &nif, 1, (void*)k_reduce_grid, dim3((unsigned)grid_reduce_ctas(s.N)), dim3(256),
+                      argsr));
+    }
+    e = cudaGraphInstantiate(exec, g, 0);
+    cudaGraphDestroy(g);
+    return e;
 }
 
 } // namespace fqsb

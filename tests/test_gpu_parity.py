@@ -287,3 +287,31 @@ def test_full_size_yields_sampled():
     s2.timeSteps(20)
     assert np.array_equal(s2.u, u1)
     assert np.array_equal(s2.chunk.index_at_align, i1)
+
+
+@pytest.mark.parametrize("kind", ["Line1d_Cuspy", "Line2d_Cuspy", "Particles_Cuspy", "Line1d_SemiSmooth",
+                                  "Line1d_Smooth"])
+def test_regeneration_inside_steps(kind):
+    """Particles slide across many wells inside minimise / flowSteps with a 40-position chunk, so chunk
+    windows move during the fused steps (the run graph's regeneration branch) -- compared with the oracle."""
+    gpu, ref = make_pair(kind, [128], nchunk=40, offset=-5.0, k_frame=0.5, eta=0.5)
+    for du in [12.0, 15.0, -20.0]:
+        gpu.u_frame = gpu.u_frame + du
+        ref.u_frame = ref.u_frame + du
+        assert gpu.minimise(time_activity=True, max_iter=200000) == ref.minimise(time_activity=True, max_iter=200000)
+        assert gpu.quasistaticActivityFirst == ref.quasistaticActivityFirst
+        assert gpu.quasistaticActivityLast == ref.quasistaticActivityLast
+        assert_same(gpu, ref)
+    gpu.flowSteps(3000, 0.2)
+    ref.flowSteps(3000, 0.2)
+    assert_same(gpu, ref)
+    assert np.max(np.abs(gpu.chunk.start)) > 20  # the windows did move
+
+
+def test_regeneration_inside_steps_large():
+    """Same at 1d N = 2^17 (many CTAs; several pending CTAs per step)."""
+    gpu, ref = make_pair("Line1d_Cuspy", [2 ** 17], nchunk=40, offset=-5.0, k_frame=0.5, eta=0.5)
+    gpu.flowSteps(800, 0.5)
+    ref.flowSteps(800, 0.5)
+    assert_same(gpu, ref)
+    assert np.max(gpu.chunk.start) > 0
