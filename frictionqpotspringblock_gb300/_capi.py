@@ -38,6 +38,7 @@ DISTRIBUTIONS = {
 }
 FIELD_U, FIELD_V, FIELD_A, FIELD_F, FIELD_F_POTENTIAL, FIELD_F_INTERACTIONS, FIELD_F_FRAME, FIELD_F_DAMPING = range(8)
 SCALAR_U_FRAME, SCALAR_T, SCALAR_TEMPERATURE, SCALAR_RESIDUAL, SCALAR_MEAN_F_FRAME = range(5)
+NOALLOC_MAX_N = 1 << 25  # FQSB_NOALLOC_MAX_N of include/fqsb.h
 
 
 class Config(ctypes.Structure):
@@ -108,6 +109,7 @@ SIGNATURES = [
     ("fqsb_get_field_device", _I, [_P, _I, _P]),
     ("fqsb_set_field_device", _I, [_P, _I, _P]),
     ("fqsb_get_stream", _I, [_P, ctypes.POINTER(_P)]),
+    ("fqsb_residual_noalloc", _I, [_P, _P, _I64, _P, _P]),
     ("fqsb_version", ctypes.c_char_p, []),
 ]
 

@@ -57,6 +57,13 @@ struct fqsb_system {
 
 static std::string g_create_error;
 
+namespace fqsb {
+void set_global_error(const std::string& msg)
+{
+    g_create_error = msg;
+}
+} // namespace fqsb
+
 static int set_err(fqsb_system* h, int code, const std::string& msg)
 {
     if (h) {

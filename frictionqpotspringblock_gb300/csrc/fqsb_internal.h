@@ -7,6 +7,8 @@
 
 #include <cuda_runtime.h>
 
+#include <string>
+
 #include "fqsb_device.cuh"
 
 namespace fqsb {
@@ -19,6 +21,9 @@ struct LineGeom {
 };
 
 LineGeom line_geometry(int64_t N);
+
+/* Message returned by fqsb_last_error(NULL) (errors of calls that have no handle). */
+void set_global_error(const std::string& msg);
 
 /* Per-particle canonical reduction of the step's residual terms (used by the 2d path). */
 int64_t grid_reduce_ctas(int64_t N);

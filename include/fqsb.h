@@ -150,6 +150,21 @@ int fqsb_set_field_device(fqsb_system* h, int field, const double* in_device);
 /* Timing support: the stream the handle launches on (a cudaStream_t). */
 int fqsb_get_stream(fqsb_system* h, void** stream);
 
+/*
+ * Residual |f| / |f_frame| (|f| when |f_frame| == 0) of two device arrays of n doubles, in the same
+ * fixed pairwise summation order as FQSB_SCALAR_RESIDUAL, written to the device double
+ * *residual_device; enqueued on `stream` (a cudaStream_t, NULL = default stream) and asynchronous,
+ * unlike the other entry points.  No counterpart in the reference: it exists for callers that cannot
+ * allocate device memory (inside a global-mode stream capture, under another framework's memory
+ * pool, or in loops that cannot afford cudaFree's implicit synchronisation).  It allocates nothing:
+ * its scratch is a fixed 512 KiB device array shared by all calls, so n <= FQSB_NOALLOC_MAX_N
+ * (larger n fails with FQSB_ERR_INVALID) and calls that overlap on the GPU race.  The first call on a
+ * device looks up the scratch address; make it before any stream capture begins.
+ */
+#define FQSB_NOALLOC_MAX_N ((int64_t)1 << 25)
+int fqsb_residual_noalloc(const double* f_device, const double* f_frame_device, int64_t n, double* residual_device,
+                          void* stream);
+
 /* Build information: "fqsb <version> sm_103a". */
 const char* fqsb_version(void);
 
