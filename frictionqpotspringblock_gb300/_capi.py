@@ -66,6 +66,30 @@ class Config(ctypes.Structure):
     ]
 
 
+class BatchConfig(ctypes.Structure):
+    _fields_ = [
+        ("n_instances", ctypes.c_int64),
+        ("sizes", ctypes.POINTER(ctypes.c_int64)),
+        ("seeds", ctypes.POINTER(ctypes.c_uint64)),
+        ("k_frame", ctypes.POINTER(ctypes.c_double)),
+        ("m", ctypes.c_double),
+        ("eta", ctypes.c_double),
+        ("mu", ctypes.c_double),
+        ("k_interactions", ctypes.c_double),
+        ("dt", ctypes.c_double),
+        ("distribution", ctypes.c_int),
+        ("n_parameters", ctypes.c_int),
+        ("parameters", ctypes.c_double * 4),
+        ("offset", ctypes.c_double),
+        ("nchunk", ctypes.c_int64),
+        ("window", ctypes.c_int64),
+        ("threads", ctypes.c_int),
+        ("ppt", ctypes.c_int),
+        ("stream", ctypes.c_void_p),
+        ("device", ctypes.c_int),
+    ]
+
+
 # (name, restype, argtypes) of every entry point of include/fqsb.h
 _P = ctypes.c_void_p
 _D = ctypes.c_double
@@ -110,6 +134,13 @@ SIGNATURES = [
     ("fqsb_set_field_device", _I, [_P, _I, _P]),
     ("fqsb_get_stream", _I, [_P, ctypes.POINTER(_P)]),
     ("fqsb_residual_noalloc", _I, [_P, _P, _I64, _P, _P]),
+    ("fqsb_batch_create", _I, [ctypes.POINTER(BatchConfig), ctypes.POINTER(_P)]),
+    ("fqsb_batch_destroy", _I, [_P]),
+    ("fqsb_batch_last_error", ctypes.c_char_p, [_P]),
+    ("fqsb_batch_quasistatic", _I, [_P, _I64, _D, _D, _U64, _U64, _PD, _PD, _PI64, _PI64, ctypes.POINTER(ctypes.c_int32)]),
+    ("fqsb_batch_get", _I, [_P, _I64, _I, _PD]),
+    ("fqsb_batch_get_index", _I, [_P, _I64, _PI64]),
+    ("fqsb_batch_frame", _I, [_P, _PD]),
     ("fqsb_version", ctypes.c_char_p, []),
 ]
 

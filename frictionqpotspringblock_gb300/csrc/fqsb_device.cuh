@@ -117,6 +117,7 @@ struct DevSys {
     double offset;
     const double* offp;
     uint64_t seed;
+    const uint64_t* pseed; /* per-particle pcg32 initstate (batched realisations), or NULL: seed + p */
     int64_t buffer, margin, min_margin;
     double* data;
     int64_t* start;
@@ -232,7 +233,7 @@ __device__ __forceinline__ void seq_origin(const DevSys& s, int64_t p, int& kind
     }
     else {
         k0 = 0;
-        st0 = pcg_seed(s.seed + (uint64_t)p);
+        st0 = pcg_seed(s.pseed ? s.pseed[p] : s.seed + (uint64_t)p);
     }
 }
 

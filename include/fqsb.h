@@ -151,6 +151,51 @@ int fqsb_set_field_device(fqsb_system* h, int field, const double* in_device);
 int fqsb_get_stream(fqsb_system* h, void** stream);
 
 /*
+ * Batched form: many independent Line1d System_Cuspy_Laplace realisations of uneven size (realisation j:
+ * sizes[j] particles, pcg32 initstate seeds[j] + p, frame stiffness k_frame[j]; shared m, eta, mu,
+ * k_interactions, dt, distribution, offset, nchunk) on one GPU.  No counterpart in the reference,
+ * which runs one System at a time; each realisation follows exactly the plain path's arithmetic.
+ * `window` (34 <= window <= nchunk) is the number of yield positions kept per particle; the yield
+ * sequence does not depend on it.  threads (32..256) x ppt (1 or 2) is the tile (0: defaults).
+ */
+typedef struct {
+    int64_t n_instances;
+    const int64_t* sizes;
+    const uint64_t* seeds;
+    const double* k_frame;
+    double m, eta, mu, k_interactions, dt;
+    int distribution;
+    int n_parameters;
+    double parameters[4];
+    double offset;
+    int64_t nchunk;
+    int64_t window;
+    int threads, ppt;
+    void* stream;
+    int device;
+} fqsb_batch_config;
+
+typedef struct fqsb_batch fqsb_batch;
+
+int fqsb_batch_create(const fqsb_batch_config* cfg, fqsb_batch** out);
+int fqsb_batch_destroy(fqsb_batch* h);
+const char* fqsb_batch_last_error(const fqsb_batch* h);
+/*
+ * ncycles quasistatic cycles per realisation, in one device-side run: each cycle is
+ * eventDrivenStep(eps, kick=false), eventDrivenStep(eps, kick=true), minimise(tol, niter_tol, max_iter)
+ * (the protocol of the reference's examples/Line1d_Cuspy_Laplace.py:41-60), every realisation
+ * converging on its own.  Per realisation and cycle (arrays [n_instances x ncycles]): u_frame, mean
+ * f_frame, the avalanche size S = sum(index_at_align - index at the cycle start) and inc after the
+ * cycle; status_out[j] = 0, FQSB_ERR_NAN or FQSB_ERR_NO_CONVERGENCE.
+ */
+int fqsb_batch_quasistatic(fqsb_batch* h, int64_t ncycles, double eps, double tol, uint64_t niter_tol,
+                           uint64_t max_iter, double* u_frame_out, double* f_frame_out, int64_t* S_out,
+                           int64_t* inc_out, int32_t* status_out);
+int fqsb_batch_get(fqsb_batch* h, int64_t instance, int field, double* out); /* u, v or a of one realisation */
+int fqsb_batch_get_index(fqsb_batch* h, int64_t instance, int64_t* index_at_align);
+int fqsb_batch_frame(fqsb_batch* h, double* u_frame); /* u_frame of every realisation */
+
+/*
  * Residual |f| / |f_frame| (|f| when |f_frame| == 0) of two device arrays of n doubles, in the same
  * fixed pairwise summation order as FQSB_SCALAR_RESIDUAL, written to the device double
  * *residual_device; enqueued on `stream` (a cudaStream_t, NULL = default stream) and asynchronous,
