@@ -134,6 +134,9 @@ SIGNATURES = [
     ("fqsb_set_field_device", _I, [_P, _I, _P]),
     ("fqsb_get_stream", _I, [_P, ctypes.POINTER(_P)]),
     ("fqsb_residual_noalloc", _I, [_P, _P, _I64, _P, _P]),
+    ("fqsb_set_parameters", _I, [_P, _D, _D, _D]),
+    ("fqsb_adjoint_forward", _I, [_P, _PD, _I64, _I64, _I64, _PD]),
+    ("fqsb_adjoint_backward", _I, [_P, _PD, _PD, _PD, _PD]),
     ("fqsb_batch_create", _I, [ctypes.POINTER(BatchConfig), ctypes.POINTER(_P)]),
     ("fqsb_batch_destroy", _I, [_P]),
     ("fqsb_batch_last_error", ctypes.c_char_p, [_P]),

@@ -306,6 +306,35 @@ class System:
     def flowSteps(self, n, v_frame):
         C.check(self._h, C.lib().fqsb_flow_steps(self._h, int(n), float(v_frame)))
 
+    # ---------------------------------------------------------------- differentiation support
+    def set_parameters(self, mu, k_interactions, eta):
+        """Change mu, k_interactions and eta of the existing system (an extension; the reference fixes
+        them at construction)."""
+        C.check(self._h, C.lib().fqsb_set_parameters(self._h, float(mu), float(k_interactions), float(eta)))
+        self._mu, self._eta = float(mu), float(eta)
+
+    def adjoint_forward(self, schedule, K=100, last=500) -> float:
+        """From the current state run len(schedule) steps with u_frame = schedule[t] set before step t,
+        keeping checkpoints every K steps; returns
+        L = mean over the last `last` steps of mean(f_frame) + 0.5 * mean(u_T**2)."""
+        sched = np.ascontiguousarray(schedule, dtype=np.float64)
+        loss = ctypes.c_double()
+        C.check(self._h, C.lib().fqsb_adjoint_forward(self._h, _ptr(sched, ctypes.c_double), len(sched), int(K),
+                                                      int(last), ctypes.byref(loss)))
+        self._adj_T = len(sched)
+        return loss.value
+
+    def adjoint_backward(self):
+        """Gradients of the last adjoint_forward's loss: (dL/du0, dL/dv0, dL/dschedule,
+        [dL/dmu, dL/dk_interactions, dL/deta])."""
+        gu = np.empty(self._size)
+        gv = np.empty(self._size)
+        gs = np.empty(self._adj_T)
+        gp = np.empty(3)
+        C.check(self._h, C.lib().fqsb_adjoint_backward(self._h, _ptr(gu, ctypes.c_double), _ptr(gv, ctypes.c_double),
+                                                       _ptr(gs, ctypes.c_double), _ptr(gp, ctypes.c_double)))
+        return gu.reshape(self._shape), gv.reshape(self._shape), gs, gp
+
     # ---------------------------------------------------------------- device access
     @property
     def stream(self) -> int:

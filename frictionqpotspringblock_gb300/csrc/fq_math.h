@@ -363,8 +363,8 @@ FQ_HD double fq_pow(double x, double y)
     return fq_exp_dd(fq_dd_mul_d(L, y));
 }
 
-/* sin(x): reduction by pi/2 in double-double, then Taylor series. */
-FQ_HD double fq_sin(double x)
+/* sin(x + shift * pi/2) for shift in {0, 1}: reduction by pi/2 in double-double, Taylor series. */
+FQ_HD double fq_sin_shift(double x, int shift)
 {
     if (x != x) {
         return x;
@@ -372,7 +372,7 @@ FQ_HD double fq_sin(double x)
     if ((fq_bits(x) & 0x7fffffffffffffffULL) == FQ_INF_BITS) {
         return fq_from_bits(FQ_NAN_BITS);
     }
-    if (x == 0.0) {
+    if (x == 0.0 && shift == 0) {
         return x;
     }
     double kf = FQ_MUL(x, FQ_TWO_OVER_PI);
@@ -380,7 +380,7 @@ FQ_HD double fq_sin(double x)
     int64_t n = (int64_t)nf;
     fq_dd r = fq_dd_add(fq_dd_make(x, 0.0), fq_dd_neg(fq_dd_mul_d(fq_dd_make(FQ_PIO2_HI, FQ_PIO2_LO), nf)));
     fq_dd r2 = fq_dd_mul(r, r);
-    int q = (int)(n & 3);
+    int q = (int)((n + shift) & 3);
     double ch, cl;
     fq_dd p;
     if (q == 0 || q == 2) {
@@ -406,6 +406,18 @@ FQ_HD double fq_sin(double x)
     }
     double y = FQ_ADD(p.hi, p.lo);
     return (q >= 2) ? -y : y;
+}
+
+/* sin(x). */
+FQ_HD double fq_sin(double x)
+{
+    return fq_sin_shift(x, 0);
+}
+
+/* cos(x) = sin(x + pi/2), the quadrant shifted exactly (no rounding of x + pi/2). */
+FQ_HD double fq_cos(double x)
+{
+    return fq_sin_shift(x, 1);
 }
 
 #endif

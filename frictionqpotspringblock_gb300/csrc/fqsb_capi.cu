@@ -53,6 +53,15 @@ struct fqsb_system {
     cudaGraphExec_t graph;
     int graph_k;
     std::string err;
+    /* adjoint tape */
+    int64_t adj_T, adj_K, adj_last, adj_nseg;
+    std::vector<double> adj_sched_host;
+    double* adj_sched;
+    double* adj_ckpt;   /* nseg x 3 x N */
+    double* adj_ffsum;  /* T */
+    double* adj_final;  /* 3 x N: state after the forward */
+    double adj_final_uframe;
+    int64_t adj_final_inc;
 };
 
 static std::string g_create_error;
@@ -205,7 +214,7 @@ __global__ void k_store_damp(DevSys d, const double* v, double* fs0, double* fs1
     }
 }
 
-enum { RED_RESIDUAL = 0, RED_VSQ = 1, RED_FFRAME = 2 };
+enum { RED_RESIDUAL = 0, RED_VSQ = 1, RED_FFRAME = 2, RED_USQ = 3 };
 
 /* level 1 of the canonical pairwise reduction: 1024 consecutive particles per CTA (4 per thread) */
 __global__ void __launch_bounds__(256) k_reduce_l1(DevSys d, int what, const double* u, const double* v, double uf,
@@ -222,6 +231,9 @@ __global__ void __launch_bounds__(256) k_reduce_l1(DevSys d, int what, const dou
         if (p < d.N) {
             if (what == RED_VSQ) {
                 x[j] = FQ_MUL(v[p], v[p]);
+            }
+            else if (what == RED_USQ) {
+                x[j] = FQ_MUL(u[p], u[p]);
             }
             else {
                 double f, ff;
@@ -546,8 +558,18 @@ struct RunResult {
  * launch of the run graph (a device-side loop); the host synchronises once (plus once per
  * RUN_BUDGET_NS of device time for long runs).
  */
+struct RunIO {
+    const double* sched = nullptr;
+    double* rec_u = nullptr;
+    double* rec_v = nullptr;
+    double* rec_a = nullptr;
+    double4_32a* rec_w = nullptr;
+    double* rec_ffsum = nullptr;
+};
+
 static int run(fqsb_system* h, int64_t max_steps, int flags, double tol, int64_t niter_tol, double vdt,
-               int64_t A_truncate, int64_t S_truncate, const int64_t* i_n_host, RunResult* res)
+               int64_t A_truncate, int64_t S_truncate, const int64_t* i_n_host, RunResult* res,
+               const RunIO* io = nullptr)
 {
     res->done = RUN_MAXITER;
     res->error = 0;
@@ -593,6 +615,14 @@ static int run(fqsb_system* h, int64_t max_steps, int flags, double tol, int64_t
     c->qs_first = h->qs_first;
     c->qs_last = h->qs_last;
     c->budget_ns = RUN_BUDGET_NS;
+    if (io) {
+        c->sched = io->sched;
+        c->rec_u = io->rec_u;
+        c->rec_v = io->rec_v;
+        c->rec_a = io->rec_a;
+        c->rec_w = io->rec_w;
+        c->rec_ffsum = io->rec_ffsum;
+    }
     if ((flags & RF_RESID) && niter_tol > 0) {
         k_fill<<<blocks_for(niter_tol, 128), 128, 0, h->stream>>>(h->d.ring, niter_tol, INFINITY);
         CU(h, cudaGetLastError());
@@ -680,7 +710,7 @@ static void free_all(fqsb_system* h)
                     d.u[0], d.u[1], d.v[0], d.v[1], d.a[0], d.a[1], d.ctl, d.ring, d.partials, d.i_n, d.sq2,
                     d.cta_pending, d.regen_list,
                     (void*)d.offp, h->scratch, h->red_partials, h->red_out, h->mkey, h->mflag, h->fs[0], h->fs[1],
-                    h->fs[2], h->fs[3], h->fs[4]};
+                    h->fs[2], h->fs[3], h->fs[4], h->adj_sched, h->adj_ckpt, h->adj_ffsum, h->adj_final};
     for (void* p : ptrs) {
         if (p) {
             cudaFree(p);
@@ -745,6 +775,10 @@ extern "C" int fqsb_create(const fqsb_config* cfg, fqsb_system** out)
     h->ring_cap = 0;
     h->graph = nullptr;
     h->graph_k = 0;
+    h->adj_T = h->adj_K = h->adj_last = h->adj_nseg = 0;
+    h->adj_sched = h->adj_ckpt = h->adj_ffsum = h->adj_final = nullptr;
+    h->adj_final_uframe = 0.0;
+    h->adj_final_inc = 0;
     h->stored = false;
     h->cur = 0;
     h->inc = 0;
@@ -1500,4 +1534,256 @@ extern "C" int fqsb_chunk_restore(fqsb_system* h, const uint64_t* state, const d
     CU(h, cudaGetLastError());
     CU(h, cudaFreeAsync(buf, h->stream));
     return sync(h);
+}
+
+/* ------------------------------------------------------------ parameters */
+
+__global__ void k_rewell(DevSys d)
+{
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < d.N) {
+        const double* y = d.data + p * d.W + d.cidx[p];
+        d.wc[p] = make_wc(d, y[0], y[1]);
+    }
+}
+
+extern "C" int fqsb_set_parameters(fqsb_system* h, double mu, double k_interactions, double eta)
+{
+    if (!h) {
+        return FQSB_ERR_INVALID;
+    }
+    h->d.mu = mu;
+    h->d.k = k_interactions;
+    h->d.me = -eta;
+    h->cfg.mu = mu;
+    h->cfg.k_interactions = k_interactions;
+    h->cfg.eta = eta;
+    h->d.s_mu = classify_scale(mu);
+    h->d.s_k = classify_scale(k_interactions);
+    /* the cached well constants of SemiSmooth depend on mu */
+    k_rewell<<<blocks_for(h->d.N, 256), 256, 0, h->stream>>>(h->d);
+    CU(h, cudaGetLastError());
+    if (h->graph) {
+        cudaGraphExecDestroy(h->graph); /* the parameters are kernel arguments of the run graph */
+        h->graph = nullptr;
+    }
+    h->stored = false;
+    return sync(h);
+}
+
+/* ------------------------------------------------------------ adjoint */
+
+static int copy_state(fqsb_system* h, double* dst3, bool to_buffer)
+{
+    size_t nb = sizeof(double) * (size_t)h->d.N;
+    int64_t N = h->d.N;
+    if (to_buffer) {
+        CU(h, cudaMemcpyAsync(dst3, cur_u(h), nb, cudaMemcpyDeviceToDevice, h->stream));
+        CU(h, cudaMemcpyAsync(dst3 + N, cur_v(h), nb, cudaMemcpyDeviceToDevice, h->stream));
+        CU(h, cudaMemcpyAsync(dst3 + 2 * N, cur_a(h), nb, cudaMemcpyDeviceToDevice, h->stream));
+    }
+    else {
+        CU(h, cudaMemcpyAsync(cur_u(h), dst3, nb, cudaMemcpyDeviceToDevice, h->stream));
+        CU(h, cudaMemcpyAsync(cur_v(h), dst3 + N, nb, cudaMemcpyDeviceToDevice, h->stream));
+        CU(h, cudaMemcpyAsync(cur_a(h), dst3 + 2 * N, nb, cudaMemcpyDeviceToDevice, h->stream));
+        int rc = updated_u(h); /* set_u: re-align the wells to the restored positions */
+        if (rc) {
+            return rc;
+        }
+    }
+    return FQSB_OK;
+}
+
+extern "C" int fqsb_adjoint_forward(fqsb_system* h, const double* schedule, int64_t T, int64_t K, int64_t last,
+                                    double* loss)
+{
+    if (!h || !schedule || !loss || T < 1 || K < 1 || last < 1 || last > T) {
+        return FQSB_ERR_INVALID;
+    }
+    if (h->is2d) {
+        return set_err(h, FQSB_ERR_UNSUPPORTED, "the adjoint is implemented for Line1d and Particles systems");
+    }
+    int64_t N = h->d.N;
+    int64_t nseg = (T + K - 1) / K;
+    for (double* p : {h->adj_sched, h->adj_ckpt, h->adj_ffsum, h->adj_final}) {
+        if (p) {
+            cudaFree(p);
+        }
+    }
+    h->adj_sched = h->adj_ckpt = h->adj_ffsum = h->adj_final = nullptr;
+    CU(h, cudaMalloc(&h->adj_sched, sizeof(double) * (size_t)T));
+    CU(h, cudaMalloc(&h->adj_ckpt, sizeof(double) * 3 * (size_t)N * (size_t)nseg));
+    CU(h, cudaMalloc(&h->adj_ffsum, sizeof(double) * (size_t)T));
+    CU(h, cudaMalloc(&h->adj_final, sizeof(double) * 3 * (size_t)N));
+    h->adj_sched_host.assign(schedule, schedule + T);
+    CU(h, cudaMemcpyAsync(h->adj_sched, schedule, sizeof(double) * (size_t)T, cudaMemcpyHostToDevice, h->stream));
+    h->adj_T = T;
+    h->adj_K = K;
+    h->adj_last = last;
+    h->adj_nseg = nseg;
+    for (int64_t seg = 0; seg < nseg; ++seg) {
+        int rc = copy_state(h, h->adj_ckpt + 3 * N * seg, true);
+        if (rc) {
+            return rc;
+        }
+        RunIO io;
+        io.sched = h->adj_sched + seg * K;
+        io.rec_ffsum = h->adj_ffsum + seg * K;
+        RunResult r;
+        rc = run(h, std::min(K, T - seg * K), RF_SCHEDULE | RF_FFSUM, 0.0, 0, 0.0, 0, 0, nullptr, &r, &io);
+        if (rc) {
+            return rc;
+        }
+    }
+    int rc = copy_state(h, h->adj_final, true);
+    if (rc) {
+        return rc;
+    }
+    h->adj_final_uframe = h->u_frame;
+    h->adj_final_inc = h->inc;
+    std::vector<double> ffs((size_t)T);
+    CU(h, cudaMemcpyAsync(ffs.data(), h->adj_ffsum, sizeof(double) * (size_t)T, cudaMemcpyDeviceToHost, h->stream));
+    double2 usq;
+    rc = reduce(h, RED_USQ, &usq); /* synchronises */
+    if (rc) {
+        return rc;
+    }
+    /* L = (1/last) sum_{t >= T-last} mean_p f_frame_t + 0.5 mean_p u_T^2 */
+    double acc = 0.0;
+    for (int64_t t = T - last; t < T; ++t) {
+        acc += ffs[(size_t)t] / (double)N;
+    }
+    *loss = acc / (double)last + 0.5 * (usq.x / (double)N);
+    return FQSB_OK;
+}
+
+__global__ void k_adj_init(const double* uT, int64_t N, double* lu, double* lv, double* la)
+{
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < N) {
+        lu[p] = FQ_DIV(uT[p], (double)N);
+        lv[p] = 0.0;
+        la[p] = 0.0;
+    }
+}
+
+extern "C" int fqsb_adjoint_backward(fqsb_system* h, double* grad_u0, double* grad_v0, double* grad_schedule,
+                                     double* grad_params)
+{
+    if (!h || !grad_u0 || !grad_v0 || !grad_schedule || !grad_params) {
+        return FQSB_ERR_INVALID;
+    }
+    if (h->adj_T < 1) {
+        return set_err(h, FQSB_ERR_INVALID, "fqsb_adjoint_backward needs a preceding fqsb_adjoint_forward");
+    }
+    const int64_t N = h->d.N, T = h->adj_T, K = h->adj_K, last = h->adj_last, nseg = h->adj_nseg;
+    const size_t nb = sizeof(double) * (size_t)N;
+    double *rec_u = nullptr, *rec_v = nullptr, *rec_a = nullptr, *lam = nullptr, *step_out = nullptr;
+    double4_32a *rec_w = nullptr, *parts = nullptr;
+    unsigned* ticket = nullptr;
+    int rc = FQSB_OK;
+    auto cleanup = [&]() {
+        for (void* p : {(void*)rec_u, (void*)rec_v, (void*)rec_a, (void*)lam, (void*)step_out, (void*)rec_w,
+                        (void*)parts, (void*)ticket}) {
+            if (p) {
+                cudaFree(p);
+            }
+        }
+    };
+#define ACU(expr)                                                                                        \
+    do {                                                                                                 \
+        cudaError_t e_ = (expr);                                                                         \
+        if (e_ != cudaSuccess) {                                                                         \
+            cleanup();                                                                                   \
+            return set_err(h, FQSB_ERR_CUDA, std::string(#expr ": ") + cudaGetErrorString(e_));          \
+        }                                                                                                \
+    } while (0)
+    ACU(cudaMalloc(&rec_u, nb * (size_t)K));
+    ACU(cudaMalloc(&rec_v, nb * (size_t)K));
+    ACU(cudaMalloc(&rec_a, nb * (size_t)K));
+    ACU(cudaMalloc(&rec_w, sizeof(double4_32a) * (size_t)N * (size_t)K));
+    ACU(cudaMalloc(&lam, nb * 6));
+    ACU(cudaMalloc(&step_out, sizeof(double) * 4 * (size_t)T));
+    ACU(cudaMalloc(&parts, sizeof(double4_32a) * (size_t)adjoint_ctas(N)));
+    ACU(cudaMalloc(&ticket, sizeof(unsigned)));
+    ACU(cudaMemsetAsync(ticket, 0, sizeof(unsigned), h->stream));
+    double* lin = lam;          /* lu, lv, la of the current step's outputs */
+    double* lout = lam + 3 * N; /* written by the step */
+    k_adj_init<<<blocks_for(N, 256), 256, 0, h->stream>>>(h->adj_final, N, lin, lin + N, lin + 2 * N);
+    ACU(cudaGetLastError());
+    const double wff = 1.0 / ((double)last * (double)N);
+    for (int64_t seg = nseg - 1; seg >= 0 && rc == FQSB_OK; --seg) {
+        const double* ck = h->adj_ckpt + 3 * N * seg;
+        rc = copy_state(h, const_cast<double*>(ck), false);
+        if (rc) {
+            break;
+        }
+        int64_t Ks = std::min(K, T - seg * K);
+        RunIO io;
+        io.sched = h->adj_sched + seg * K;
+        io.rec_u = rec_u;
+        io.rec_v = rec_v;
+        io.rec_a = rec_a;
+        io.rec_w = rec_w;
+        RunResult r;
+        rc = run(h, Ks, RF_SCHEDULE | RF_RECORD, 0.0, 0, 0.0, 0, 0, nullptr, &r, &io);
+        if (rc) {
+            break;
+        }
+        for (int64_t t = Ks - 1; t >= 0; --t) {
+            int64_t gt = seg * K + t;
+            AdjArgs A;
+            if (t == 0) {
+                A.u_in = ck;
+                A.v_in = ck + N;
+                A.a_in = ck + 2 * N;
+            }
+            else {
+                A.u_in = rec_u + (size_t)(t - 1) * N;
+                A.v_in = rec_v + (size_t)(t - 1) * N;
+                A.a_in = rec_a + (size_t)(t - 1) * N;
+            }
+            A.up = rec_u + (size_t)t * N;
+            A.w = rec_w + (size_t)t * N;
+            A.uf = h->adj_sched_host[(size_t)gt];
+            A.wff = gt >= T - last ? wff : 0.0;
+            A.lu_out = lin;
+            A.lv_out = lin + N;
+            A.la_out = lin + 2 * N;
+            A.lu_in = lout;
+            A.lv_in = lout + N;
+            A.la_in = lout + 2 * N;
+            A.partials = parts;
+            A.step_out = step_out + 4 * gt;
+            A.ticket = ticket;
+            ACU(launch_adjoint_step(h->d, A, h->stream));
+            std::swap(lin, lout);
+        }
+    }
+    if (rc) {
+        cleanup();
+        return rc;
+    }
+    std::vector<double> so((size_t)(4 * T));
+    ACU(cudaMemcpyAsync(grad_u0, lin, nb, cudaMemcpyDeviceToHost, h->stream));
+    ACU(cudaMemcpyAsync(grad_v0, lin + N, nb, cudaMemcpyDeviceToHost, h->stream));
+    ACU(cudaMemcpyAsync(so.data(), step_out, sizeof(double) * 4 * (size_t)T, cudaMemcpyDeviceToHost, h->stream));
+    ACU(cudaStreamSynchronize(h->stream));
+    double gmu = 0.0, gk = 0.0, geta = 0.0;
+    for (int64_t t = 0; t < T; ++t) {
+        grad_schedule[t] = so[(size_t)(4 * t)];
+        geta += so[(size_t)(4 * t + 1)];
+        gmu += so[(size_t)(4 * t + 2)];
+        gk += so[(size_t)(4 * t + 3)];
+    }
+    grad_params[0] = gmu;
+    grad_params[1] = gk;
+    grad_params[2] = geta;
+    /* leave the system in the forward's final state */
+    rc = copy_state(h, h->adj_final, false);
+    h->u_frame = h->adj_final_uframe;
+    h->inc = h->adj_final_inc;
+    cleanup();
+#undef ACU
+    return rc ? rc : sync(h);
 }

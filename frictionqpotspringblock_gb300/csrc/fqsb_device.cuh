@@ -55,7 +55,10 @@ enum : int { DERR_NONE = 0, DERR_NAN = 1, DERR_WALK = 5 };
  * (flagging Ctl::walk_flag) instead of running for an unbounded time. */
 constexpr int64_t MAX_WALK = int64_t(1) << 26;
 /* run flags (Ctl::flags) */
-enum : int { RF_RESID = 1, RF_ACT = 2, RF_FLOW = 4, RF_EVENT = 8, RF_TRUNCATE = 16 };
+enum : int { RF_RESID = 1, RF_ACT = 2, RF_FLOW = 4, RF_EVENT = 8, RF_TRUNCATE = 16,
+             RF_SCHEDULE = 32, /* u_frame of step i is sched[i] (set before the step, as set_u_frame) */
+             RF_RECORD = 64,   /* record each step's output u, v, a and well into rec_* [step][N] */
+             RF_FFSUM = 128 }; /* record each step's sum of f_frame (pairwise order) into rec_ffsum[step] */
 
 /* Control block of a stepping run; lives in device memory, written by the host before a run and
  * by the last CTA of every step. */
@@ -94,6 +97,11 @@ struct Ctl {
     int64_t qs_first, qs_last;
     /* last residual (for diagnostics) */
     double last_residual;
+    /* trajectory recording for the adjoint (RF_SCHEDULE / RF_RECORD / RF_FFSUM) */
+    const double* sched;
+    double *rec_u, *rec_v, *rec_a;
+    double4_32a* rec_w;
+    double* rec_ffsum;
 };
 
 /* How a multiplication by a positive parameter c is carried out (all exact-equivalent to x * c). */

@@ -35,6 +35,23 @@ int64_t step_ctas(const DevSys& s, const LineGeom& g);
  * Writes the conditional handles into s (they are kernel arguments of the graph's nodes). */
 cudaError_t build_run_graph(DevSys& s, const LineGeom& g, cudaGraphExec_t* exec);
 
+/* Arguments of one backward step of the adjoint (fqsb_adjoint.cu). */
+struct AdjArgs {
+    const double *u_in, *v_in, *a_in; /* input state of the step */
+    const double* up;                 /* output positions of the step */
+    const double4_32a* w;             /* wells used by the step */
+    double uf;                        /* u_frame of the step */
+    double wff;                       /* dL / d f_frame[p] of the step (loss window) */
+    const double *lu_out, *lv_out, *la_out;
+    double *lu_in, *lv_in, *la_in;
+    double4_32a* partials; /* per CTA */
+    double* step_out;      /* 4 doubles: sum k_frame dL/df_frame, dL/deta, dL/dmu, dL/dk of the step */
+    unsigned* ticket;
+};
+
+cudaError_t launch_adjoint_step(const DevSys& s, const AdjArgs& A, cudaStream_t st);
+int64_t adjoint_ctas(int64_t N);
+
 } // namespace fqsb
 
 #endif

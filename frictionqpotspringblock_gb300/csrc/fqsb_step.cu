@@ -99,6 +99,12 @@ __device__ void finalize_step(const DevSys& s, double uf, double sf, double sff)
     c->ticket_redo = 0;
     c->n_pending_cta = 0;
     c->n_regen = 0;
+    if (flags & RF_FFSUM) {
+        c->rec_ffsum[c->step] = sf;
+    }
+    if (flags & RF_SCHEDULE) {
+        c->u_frame = uf;
+    }
     c->step += 1;
     c->inc += 1;
     c->cur ^= 1;
@@ -236,6 +242,9 @@ __device__ __forceinline__ bool step_prologue(const DevSys& s, StepShared& sh, b
         if (sh.flags & RF_FLOW) {
             uf = FQ_ADD(uf, c->vdt);
         }
+        if (sh.flags & RF_SCHEDULE) {
+            uf = c->sched[c->step];
+        }
         sh.uf = uf;
         sh.nan = 0;
         sh.pending = 0;
@@ -330,7 +339,7 @@ enum : int {
  */
 __device__ __forceinline__ void step_epilogue(const DevSys& s, StepShared& sh, int mode, double rf, double rff)
 {
-    const bool resid = (sh.flags & RF_RESID) != 0;
+    const bool resid = (sh.flags & (RF_RESID | RF_FFSUM)) != 0;
     const bool tree = resid && mode != EPI_GRID_STEP;
     double sf = 0.0, sff = 0.0;
     if (tree) {
@@ -424,6 +433,9 @@ __global__ void __launch_bounds__(256) k_step_line(DevSys s, int redo)
     const int cur = sh.cur;
     const bool act = (sh.flags & (RF_ACT | RF_TRUNCATE | RF_EVENT)) != 0;
     const bool resid = (sh.flags & RF_RESID) != 0;
+    const bool ffsum = (sh.flags & RF_FFSUM) != 0;
+    const bool record = (sh.flags & RF_RECORD) != 0;
+    const int64_t rec_step = record ? ((volatile Ctl*)s.ctl)->step : 0;
     const double uf = sh.uf;
     const int64_t N = s.N;
     const int T = blockDim.x;
@@ -501,6 +513,16 @@ __global__ void __launch_bounds__(256) k_step_line(DevSys s, int redo)
                 rf = FQ_ADD(rf, f2);
                 rff = FQ_ADD(rff, ff2);
             }
+        }
+        else if (ffsum) {
+            rf = j == 0 ? ff : FQ_ADD(rf, ff);
+        }
+        if (record) {
+            size_t o = (size_t)rec_step * (size_t)N + (size_t)p;
+            s.ctl->rec_u[o] = up;
+            s.ctl->rec_v[o] = vo[j];
+            s.ctl->rec_a[o] = ao[j];
+            s.ctl->rec_w[o] = w;
         }
     }
     if (p0 < N) {

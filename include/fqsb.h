@@ -151,6 +151,25 @@ int fqsb_set_field_device(fqsb_system* h, int field, const double* in_device);
 int fqsb_get_stream(fqsb_system* h, void** stream);
 
 /*
+ * Parameters mu, k_interactions and eta of an existing system (no counterpart in the reference, whose
+ * parameters are fixed at construction; needed to differentiate with respect to them).
+ */
+int fqsb_set_parameters(fqsb_system* h, double mu, double k_interactions, double eta);
+
+/*
+ * Adjoint of a trajectory (no counterpart in the reference).  From the current state x_0 = (u, v, a),
+ * fqsb_adjoint_forward runs T steps with u_frame = schedule[t] set before step t (host array of T),
+ * keeps checkpoints every K steps, and returns
+ *     loss = (1/last) sum_{t = T-last}^{T-1} mean_p f_frame_t[p] + 0.5 mean_p u_T[p]^2 ;
+ * the system is left in x_T.  fqsb_adjoint_backward then recomputes each K-step segment from its
+ * checkpoint and runs the hand-written adjoint step backwards, giving dL/du_0, dL/dv_0 (host arrays of
+ * N), dL/dschedule (host array of T) and grad_params = {dL/dmu, dL/dk_interactions, dL/deta}.
+ * Exact for Smooth and SemiSmooth; for Cuspy the wells are held at the forward's.  Line1d / Particles.
+ */
+int fqsb_adjoint_forward(fqsb_system* h, const double* schedule, int64_t T, int64_t K, int64_t last, double* loss);
+int fqsb_adjoint_backward(fqsb_system* h, double* grad_u0, double* grad_v0, double* grad_schedule, double* grad_params);
+
+/*
  * Batched form: many independent Line1d System_Cuspy_Laplace realisations of uneven size (realisation j:
  * sizes[j] particles, pcg32 initstate seeds[j] + p, frame stiffness k_frame[j]; shared m, eta, mu,
  * k_interactions, dt, distribution, offset, nchunk) on one GPU.  No counterpart in the reference,

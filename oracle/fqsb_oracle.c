@@ -148,6 +148,7 @@ double oq_math(int which, double x, double y, int math_mode)
         case 1: return m_pow(x, y, math_mode);
         case 2: return m_sin(x, math_mode);
         case 3: return math_mode == OQ_MATH_PORTABLE ? fq_exp(x) : exp(x);
+        case 4: return math_mode == OQ_MATH_PORTABLE ? fq_cos(x) : cos(x);
         default: return NAN;
     }
 }

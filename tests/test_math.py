@@ -102,3 +102,13 @@ def test_exp():
         exact = float(mpmath.exp(mpmath.mpf(float(x))))
         worst = max(worst, ulp_diff(O.math("exp", float(x)), exact))
     assert worst <= 1
+
+
+def test_cos_range():
+    mpmath.mp.prec = 200
+    rng = np.random.default_rng(6)
+    worst = 0
+    for x in np.concatenate([rng.uniform(-math.pi, math.pi, 3000), [0.0, math.pi / 2, -math.pi, math.pi]]):
+        exact = float(mpmath.cos(mpmath.mpf(float(x))))
+        worst = max(worst, ulp_diff(O.math("cos", float(x)), exact))
+    assert worst <= 1
