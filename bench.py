@@ -49,6 +49,9 @@ PAR = dict(m=1.0, eta=0.1, mu=1.0, k_interactions=1.0, dt=0.1, seed=1, distribut
            parameters=[2.0, 1.0, 1e-5], offset=-100.0, nchunk=2000)
 V_FRAME = 1e-3  # u_frame += v_frame * dt = 1e-4 per step
 BYTES_PER_PARTICLE_STEP = 64  # read+write u, v, a (48 B) + read the current well {y_left, y_right} (16 B)
+# DRAM bytes per particle per step of the step kernel from one ncu capture (N = 2^21, dram__bytes_read.sum
+# + dram__bytes_write.sum = 147.49 MB per launch; profiles/k_step_line_cuspy_laplace1d_N4M.md), scaled by N
+TRAFFIC_BYTES_PER_PARTICLE_STEP = 147.49e6 / 2097152
 FP64_OPS_PER_PARTICLE_STEP = 24  # fp64 add/mul of the exact-order step; compares and 2^k scalings run on the integer pipe
 
 
@@ -113,6 +116,94 @@ class ClockSampler:
         os.unlink(self.path)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def bench_batched(fqsb, n_inst=512, n_loop=32):
+    """Batched form on the first n_inst realisations of the 4096-realisation size list (log-uniform in
+    [256, 65536] from pcg32 seed 3; seed 1000+j; k_frame = 1/N_j; Weibull(2,1)+1e-5; 1000-position
+    chunk), one quasistatic cycle each; against looping the plain path over the first n_loop."""
+    from frictionqpotspringblock_gb300 import batch as B
+
+    par = dict(m=1.0, eta=0.1, mu=1.0, k_interactions=1.0, dt=0.1, distribution="weibull",
+               parameters=[2.0, 1.0, 1e-5], offset=-100.0)
+    sizes = B.log_uniform_sizes(4096, 256, 65536, seed=3)
+    seeds = 1000 + np.arange(4096)
+    out = {}
+    b = B.Line1d_System_Cuspy_Laplace(sizes[:n_inst], seeds[:n_inst], 1.0 / sizes[:n_inst], nchunk=1000, window=64,
+                                      threads=256, ppt=1, **par)
+    t0 = time.perf_counter()
+    r = b.quasistatic(1, 1e-5)
+    t = time.perf_counter() - t0
+    ps = int((r["inc"][:, -1] * sizes[:n_inst]).sum())
+    out.update(realisations=n_inst, particles=int(sizes[:n_inst].sum()), seconds=t, particle_steps=ps, value=ps / t)
+    del b
+    b = B.Line1d_System_Cuspy_Laplace(sizes[:n_loop], seeds[:n_loop], 1.0 / sizes[:n_loop], nchunk=1000, window=64,
+                                      threads=256, ppt=1, **par)
+    t0 = time.perf_counter()
+    r = b.quasistatic(1, 1e-5)
+    tb = time.perf_counter() - t0
+    del b
+    tp = 0.0
+    for j in range(n_loop):
+        s = fqsb.Line1d.System_Cuspy_Laplace(k_frame=1.0 / float(sizes[j]), shape=[int(sizes[j])], seed=int(seeds[j]),
+                                             nchunk=1000, **par)
+        t0 = time.perf_counter()
+        s.eventDrivenStep(1e-5, False)
+        s.eventDrivenStep(1e-5, True)
+        s.minimise()
+        tp += time.perf_counter() - t0
+        del s
+    out.update(loop_realisations=n_loop, loop_plain_seconds=tp, loop_batched_seconds=tb, speedup_vs_plain_loop=tp / tb)
+    return out
+
+
+def bench_adjoint(fqsb, N=65536, T=5000, K=100, last=500):
+    """Adjoint of the differentiation workload: Line1d System_Smooth_Laplace, N = 65536, k_frame = 1/N,
+    Weibull(2,1)+1e-5 seed 4, u0 = v0 = 0, u_frame(t) = 1e-3 t + 0.05 sin(2 pi t / 500), T = 5000,
+    checkpoints every 100 steps; forward vs forward + backward wall time."""
+    s = fqsb.Line1d.System_Smooth_Laplace(m=1.0, eta=0.1, mu=1.0, k_interactions=1.0, k_frame=1.0 / N, dt=0.1,
+                                          shape=[N], seed=4, distribution="weibull", parameters=[2.0, 1.0, 1e-5],
+                                          offset=-100.0, nchunk=1000)
+    t = np.arange(T)
+    sched = 1e-3 * t + 0.05 * np.sin(2 * np.pi * t / 500)
+    zero = np.zeros(N)
+    for _ in range(2):
+        s.u, s.v, s.a = zero, zero, zero
+        s.adjoint_forward(sched, K=K, last=last)
+    s.u, s.v, s.a = zero, zero, zero
+    t0 = time.perf_counter()
+    loss = s.adjoint_forward(sched, K=K, last=last)
+    tf = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    gu, gv, gs, gp = s.adjoint_backward()
+    tb = time.perf_counter() - t0
+    return {"particles": N, "steps": T, "checkpoint_every": K, "loss": loss, "forward_s": tf, "backward_s": tb,
+            "backward_over_forward": tb / tf, "total_over_forward": (tf + tb) / tf,
+            "grad_norms": {"u0": float(np.linalg.norm(gu)), "schedule": float(np.linalg.norm(gs)),
+                           "params": [float(x) for x in gp]}}
+
+
+def bench_small(fqsb, cycles=20):
+    """Small system: Line1d System_Cuspy_Laplace N = 1024, k_frame = 1/1024, Weibull(2,1)+1e-5 seed 0,
+    1000-position chunk shifted per particle so that u = 0 is the centre of well 500; cycles of
+    eventDrivenStep(1e-5, kick=False), eventDrivenStep(1e-5, kick=True), minimise(tol=1e-5)."""
+    par = dict(m=1.0, eta=0.1, mu=1.0, k_interactions=1.0, k_frame=1.0 / 1024, dt=0.1, shape=[1024], seed=0,
+               distribution="weibull", parameters=[2.0, 1.0, 1e-5], nchunk=1000)
+    raw = fqsb.Line1d.System_Cuspy_Laplace(offset=0.0, **par).chunk.data
+    offp = -0.5 * (raw[:, 500] + raw[:, 501])
+    s = fqsb.Line1d.System_Cuspy_Laplace(offset=0.0, offset_per_particle=offp, **par)
+    s.eventDrivenStep(1e-5, False)
+    s.eventDrivenStep(1e-5, True)
+    s.minimise(max_iter=1000000)
+    inc0 = s.inc
+    t0 = time.perf_counter()
+    for _ in range(cycles):
+        s.eventDrivenStep(1e-5, False)
+        s.eventDrivenStep(1e-5, True)
+        s.minimise(max_iter=1000000)
+    t = time.perf_counter() - t0
+    return {"particles": 1024, "cycles": cycles, "seconds_per_cycle": t / cycles,
+            "steps_per_cycle": (s.inc - inc0) / cycles, "us_per_step": 1e6 * t / max(1, s.inc - inc0)}
 
 
 def cpu_baseline_sample(n_sample=2 ** 16, steps=3000, repeats=1):
@@ -201,6 +292,7 @@ def main():
     ap.add_argument("--nchunk", type=int, default=2000, help="yield positions per particle (profiling cases only)")
     ap.add_argument("--no-minimise", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true", help="skip the batched / adjoint / small-system extras")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -299,6 +391,12 @@ def main():
         barrier()
         minimise = {"seconds": time.perf_counter() - t0, "steps": system.inc - inc0, "ret": ret}
 
+    forms = {}
+    if not args.no_forms:
+        forms["batched"] = bench_batched(fqsb)
+        forms["adjoint"] = bench_adjoint(fqsb)
+        forms["small_system"] = bench_small(fqsb)
+
     if rank != 0:
         return
     cpu = None
@@ -327,7 +425,8 @@ def main():
                 "d2h_bytes_per_step": 8 * N},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved_gbs / hbm_peak, "traffic": None, "peak_kind": peak_kind,
+                     "frac": achieved_gbs / hbm_peak, "traffic": TRAFFIC_BYTES_PER_PARTICLE_STEP * N,
+                     "traffic_unit": "bytes per launch (ncu capture at N=2^21 scaled by N)", "peak_kind": peak_kind,
                      "algorithmic_bytes_per_particle_step": BYTES_PER_PARTICLE_STEP,
                      "kernel": "k_step_line<Cuspy, Laplace1d, units, 2 per thread>",
                      "kernel_us": kernel_s * 1e6},
@@ -338,6 +437,7 @@ def main():
         "clocks": clk,
         "wall_s": t_wall,
         "minimise": minimise,
+        "forms": forms,
         "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)

@@ -43,8 +43,18 @@ __device__ __forceinline__ AdjTerms adj_particle(const DevSys& s, const AdjArgs&
     (void)u;
     double up = A.up[p];
     double4_32a w = A.w[p];
-    /* forward intermediates */
-    double fp = pot_force<POT>(s, w, up);
+    /* forward intermediates.  Smooth: sin and cos of the phase from one sincos call; the adjoint needs
+     * them to the gradient tolerance only (the forward's bit-exact sine is not needed here) */
+    double fp, sn = 0.0, cs = 0.0;
+    if (POT == POT_SMOOTH) {
+        const double pi = 3.14159265358979323846;
+        double arg = FQ_DIV(FQ_MUL(pi, FQ_SUB(up, w.z)), w.w);
+        sincos(arg, &sn, &cs);
+        fp = FQ_MUL(FQ_DIV(FQ_MUL(-s.mu, w.w), pi), sn);
+    }
+    else {
+        fp = pot_force<POT>(s, w, up);
+    }
     double ff = scale(FQ_SUB(A.uf, up), s.s_kf);
     double lap = 0.0, fi = 0.0;
     if (INTER == INTER_LAPLACE1D) {
@@ -97,9 +107,8 @@ __device__ __forceinline__ AdjTerms adj_particle(const DevSys& s, const AdjArgs&
     }
     else {
         const double pi = 3.14159265358979323846;
-        double arg = FQ_DIV(FQ_MUL(pi, FQ_SUB(up, w.z)), w.w);
-        dfdu = -FQ_MUL(s.mu, fq_cos(arg));
-        dfdmu = FQ_MUL(FQ_DIV(-w.w, pi), fq_sin(arg));
+        dfdu = -FQ_MUL(s.mu, cs);
+        dfdmu = FQ_MUL(FQ_DIV(-w.w, pi), sn);
     }
     r.sbar = sb;
     r.upbar = FQ_ADD(FQ_SUB(A.lu_out[p], scale(ffb, s.s_kf)), FQ_MUL(dfdu, sb));

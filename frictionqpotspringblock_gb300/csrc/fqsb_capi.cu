@@ -13,6 +13,7 @@
  * and f) until the next operation that calls updated_u.
  */
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -52,6 +53,7 @@ struct fqsb_system {
     int64_t ring_cap;
     cudaGraphExec_t graph;
     int graph_k;
+    bool use_graph; /* false when FQSB_NO_GRAPH=1: host-driven launches (profiling) */
     std::string err;
     /* adjoint tape */
     int64_t adj_T, adj_K, adj_last, adj_nseg;
@@ -540,6 +542,10 @@ static const int64_t RING_MIN = 1024;
 
 static int ensure_graph(fqsb_system* h)
 {
+    if (!h->use_graph) {
+        h->d.in_graph = 0;
+        return FQSB_OK;
+    }
     if (h->graph) {
         return FQSB_OK;
     }
@@ -644,7 +650,14 @@ static int run(fqsb_system* h, int64_t max_steps, int flags, double tol, int64_t
         CU(h, cudaGetLastError());
     }
     for (;;) {
-        CU(h, cudaGraphLaunch(h->graph, h->stream));
+        if (h->use_graph) {
+            CU(h, cudaGraphLaunch(h->graph, h->stream));
+        }
+        else {
+            for (int i = 0; i < 64; ++i) {
+                CU(h, launch_iteration(h->d, h->lg, h->stream));
+            }
+        }
         CU(h, cudaMemcpyAsync(c, h->d.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, h->stream));
         rc = sync(h);
         if (rc) {
@@ -775,6 +788,10 @@ extern "C" int fqsb_create(const fqsb_config* cfg, fqsb_system** out)
     h->ring_cap = 0;
     h->graph = nullptr;
     h->graph_k = 0;
+    {
+        const char* ng = getenv("FQSB_NO_GRAPH");
+        h->use_graph = !(ng && ng[0] == '1');
+    }
     h->adj_T = h->adj_K = h->adj_last = h->adj_nseg = 0;
     h->adj_sched = h->adj_ckpt = h->adj_ffsum = h->adj_final = nullptr;
     h->adj_final_uframe = 0.0;

@@ -152,6 +152,7 @@ struct DevSys {
     int32_t* regen_list;  /* particles whose chunk window must move (capacity N) */
     unsigned long long h_while; /* cudaGraphConditionalHandle of the run loop */
     unsigned long long h_if;    /* cudaGraphConditionalHandle of the regeneration branch */
+    int in_graph;               /* 0: kernels launched one by one by the host (no conditional handles) */
 };
 
 /* ------------------------------------------------------------ pcg32 */

@@ -35,6 +35,9 @@ int64_t step_ctas(const DevSys& s, const LineGeom& g);
  * Writes the conditional handles into s (they are kernel arguments of the graph's nodes). */
 cudaError_t build_run_graph(DevSys& s, const LineGeom& g, cudaGraphExec_t* exec);
 
+/* One loop iteration launched kernel by kernel by the host (s.in_graph must be 0). */
+cudaError_t launch_iteration(const DevSys& s, const LineGeom& g, cudaStream_t st);
+
 /* Arguments of one backward step of the adjoint (fqsb_adjoint.cu). */
 struct AdjArgs {
     const double *u_in, *v_in, *a_in; /* input state of the step */

@@ -84,7 +84,16 @@ __device__ __forceinline__ uint64_t globaltimer()
 
 __device__ __forceinline__ void set_loop(const DevSys& s, unsigned v)
 {
-    cudaGraphSetConditional((cudaGraphConditionalHandle)s.h_while, v);
+    if (s.in_graph) {
+        cudaGraphSetConditional((cudaGraphConditionalHandle)s.h_while, v);
+    }
+}
+
+__device__ __forceinline__ void set_branch(const DevSys& s, unsigned v)
+{
+    if (s.in_graph) {
+        cudaGraphSetConditional((cudaGraphConditionalHandle)s.h_if, v);
+    }
 }
 
 /*
@@ -388,12 +397,12 @@ __device__ __forceinline__ void step_epilogue(const DevSys& s, StepShared& sh, i
         if (pend || mode == EPI_GRID_STEP) {
             if (tid == 0) {
                 c->ticket = 0;
-                cudaGraphSetConditional((cudaGraphConditionalHandle)s.h_if, pend ? 1u : 0u);
+                set_branch(s, pend ? 1u : 0u);
             }
             return;
         }
         if (tid == 0) {
-            cudaGraphSetConditional((cudaGraphConditionalHandle)s.h_if, 0u);
+            set_branch(s, 0u);
         }
     }
     double2 tot = make_double2(0.0, 0.0);
@@ -804,6 +813,41 @@ static cudaError_t add_conditional(cudaGraphNode_t* node, cudaGraph_t graph, con
     return e;
 }
 
+/*
+ * Host-driven form of one loop iteration (no conditional nodes, e.g. for profilers that cannot
+ * profile kernels inside conditional graphs): pass 1, the regeneration kernel and the redo are always
+ * launched; the latter two do nothing when no CTA is pending.
+ */
+cudaError_t launch_iteration(const DevSys& s, const LineGeom& g0, cudaStream_t st)
+{
+    bool is2d = s.inter == INTER_LAPLACE2D;
+    dim3 grid, block;
+    if (is2d) {
+        grid = dim3((unsigned)((s.cols + 31) / 32), (unsigned)((s.rows + 7) / 8));
+        block = dim3(32, 8);
+    }
+    else {
+        grid = dim3((unsigned)g0.grid);
+        block = dim3((unsigned)g0.threads);
+    }
+    void* fstep = step_kernel(s, g0);
+    int pass1 = 0, pass2 = 1;
+    void* args1[] = {(void*)&s, (void*)&pass1};
+    void* args2[] = {(void*)&s, (void*)&pass2};
+    void* argsr[] = {(void*)&s};
+    cudaError_t e = cudaLaunchKernel(fstep, grid, block, args1, 0, st);
+    if (e == cudaSuccess) {
+        e = cudaLaunchKernel((void*)k_regen, dim3(4 * 152), dim3(128), argsr, 0, st);
+    }
+    if (e == cudaSuccess) {
+        e = cudaLaunchKernel(fstep, grid, block, args2, 0, st);
+    }
+    if (e == cudaSuccess && is2d) {
+        e = cudaLaunchKernel((void*)k_reduce_grid, dim3((unsigned)grid_reduce_ctas(s.N)), dim3(256), argsr, 0, st);
+    }
+    return e;
+}
+
 #define GR(expr)                                                                                       \
     do {                                                                                               \
         cudaError_t e_ = (expr);                                                                       \
@@ -832,6 +876,7 @@ cudaError_t build_run_graph(DevSys& s, const LineGeom& g0, cudaGraphExec_t* exec
     GR(cudaGraphConditionalHandleCreate(&hi, body, 0, cudaGraphCondAssignDefault));
     s.h_while = hw;
     s.h_if = hi;
+    s.in_graph = 1;
 
     bool is2d = s.inter == INTER_LAPLACE2D;
     dim3 grid, block;
