@@ -52,7 +52,10 @@ BYTES_PER_PARTICLE_STEP = 64  # read+write u, v, a (48 B) + read the current wel
 # DRAM bytes per particle per step of the step kernel from one ncu capture (N = 2^21, dram__bytes_read.sum
 # + dram__bytes_write.sum = 147.49 MB per launch; profiles/k_step_line_cuspy_laplace1d_N4M.md), scaled by N
 TRAFFIC_BYTES_PER_PARTICLE_STEP = 147.49e6 / 2097152
-FP64_OPS_PER_PARTICLE_STEP = 24  # fp64 add/mul of the exact-order step; compares and 2^k scalings run on the integer pipe
+FP64_OPS_PER_PARTICLE_STEP = 24  # binary64 add/mul of the exact-order step; compares and 2^k scalings are integer work
+# of those, the step kernel issues these on the fp64 pipe; the rest (the 8 multiplications and the 2 additions of
+# the position update) run bit-identically on the integer pipes (csrc/fq_soft64.h)
+FP64_PIPE_OPS_PER_PARTICLE_STEP = 14
 
 
 def workload(n):
@@ -183,7 +186,7 @@ def bench_adjoint(fqsb, N=65536, T=5000, K=100, last=500):
                            "params": [float(x) for x in gp]}}
 
 
-def bench_small(fqsb, cycles=20):
+def bench_small(fqsb, cycles=20, cpu_cycles=3):
     """Small system: Line1d System_Cuspy_Laplace N = 1024, k_frame = 1/1024, Weibull(2,1)+1e-5 seed 0,
     1000-position chunk shifted per particle so that u = 0 is the centre of well 500; cycles of
     eventDrivenStep(1e-5, kick=False), eventDrivenStep(1e-5, kick=True), minimise(tol=1e-5)."""
@@ -202,8 +205,27 @@ def bench_small(fqsb, cycles=20):
         s.eventDrivenStep(1e-5, True)
         s.minimise(max_iter=1000000)
     t = time.perf_counter() - t0
-    return {"particles": 1024, "cycles": cycles, "seconds_per_cycle": t / cycles,
-            "steps_per_cycle": (s.inc - inc0) / cycles, "us_per_step": 1e6 * t / max(1, s.inc - inc0)}
+    out = {"particles": 1024, "cycles": cycles, "seconds_per_cycle": t / cycles,
+           "steps_per_cycle": (s.inc - inc0) / cycles, "us_per_step": 1e6 * t / max(1, s.inc - inc0)}
+    if cpu_cycles > 0:
+        # the same protocol on the CPU oracle (the reference restated: libm, sequential sums), one core
+        from oracle import oracle as O
+
+        r = O.line1d("Cuspy", offset=0.0, offset_per_particle=offp, sum_mode=O.SUM_SEQUENTIAL, math_mode=O.MATH_LIBM,
+                     **par)
+        r.eventDrivenStep(1e-5, False)
+        r.eventDrivenStep(1e-5, True)
+        r.minimise(max_iter=1000000)
+        inc0 = r.inc
+        t0 = time.perf_counter()
+        for _ in range(cpu_cycles):
+            r.eventDrivenStep(1e-5, False)
+            r.eventDrivenStep(1e-5, True)
+            r.minimise(max_iter=1000000)
+        tc = time.perf_counter() - t0
+        out["cpu_oracle"] = {"cycles": cpu_cycles, "cores": 1, "us_per_step": 1e6 * tc / max(1, r.inc - inc0)}
+        out["speedup_vs_cpu_oracle"] = out["cpu_oracle"]["us_per_step"] / out["us_per_step"]
+    return out
 
 
 def cpu_baseline_sample(n_sample=2 ** 16, steps=3000, repeats=1):
@@ -431,9 +453,13 @@ def main():
                      "kernel": "k_step_line<Cuspy, Laplace1d, units, 2 per thread>",
                      "kernel_us": kernel_s * 1e6},
         "fp64": {"ops_per_particle_step": FP64_OPS_PER_PARTICLE_STEP,
+                 "ops_on_fp64_pipe": FP64_PIPE_OPS_PER_PARTICLE_STEP,
+                 "ops_on_integer_pipes": FP64_OPS_PER_PARTICLE_STEP - FP64_PIPE_OPS_PER_PARTICLE_STEP,
                  "achieved_gops": FP64_OPS_PER_PARTICLE_STEP * N / kernel_s / 1e9,
+                 "fp64_pipe_gops": FP64_PIPE_OPS_PER_PARTICLE_STEP * N / kernel_s / 1e9,
                  "peak_gops": 505.0, "peak_source": "profiles/fp64_throughput_gb300.md",
-                 "frac": FP64_OPS_PER_PARTICLE_STEP * N / kernel_s / 1e9 / 505.0},
+                 "frac": FP64_OPS_PER_PARTICLE_STEP * N / kernel_s / 1e9 / 505.0,
+                 "frac_fp64_pipe": FP64_PIPE_OPS_PER_PARTICLE_STEP * N / kernel_s / 1e9 / 505.0},
         "clocks": clk,
         "wall_s": t_wall,
         "minimise": minimise,

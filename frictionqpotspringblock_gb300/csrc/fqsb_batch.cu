@@ -268,7 +268,7 @@ __device__ void batch_iteration_end(const BatchDev& b, bool redo)
  * neighbours on the realisation's ring come from shared memory or are recomputed at the tile edges.
  */
 template <int PPT>
-__global__ void __launch_bounds__(256) k_batch(BatchDev b, int redo)
+__global__ void __launch_bounds__(256, 4) k_batch(BatchDev b, int redo)
 {
     __shared__ BShared sh;
     __shared__ double sh_un[256 * PPT];
@@ -312,6 +312,7 @@ __global__ void __launch_bounds__(256) k_batch(BatchDev b, int redo)
     bool pending = false;
 
     if (phase == PH_MIN_STEP) {
+        constexpr unsigned SOFT = STEP_SOFT; /* fp64 / integer-pipe split of the step's operations */
         const double uf = sh.uf;
         const Scale skf = I->s_kf;
         double un[PPT], vr[PPT], ar[PPT];
@@ -320,7 +321,7 @@ __global__ void __launch_bounds__(256) k_batch(BatchDev b, int redo)
             int64_t g = off + l0 + q;
             vr[q] = v0[g];
             ar[q] = a0[g];
-            un[q] = FQ_ADD(FQ_ADD(u0[g], FQ_MUL(s.dt, vr[q])), FQ_MUL(s.hdt2, ar[q]));
+            un[q] = S_ADD(3, S_ADD(2, u0[g], S_MUL(0, s.dt, vr[q])), S_MUL(1, s.hdt2, ar[q]));
             sh_un[threadIdx.x * PPT + q] = un[q];
         }
         __syncthreads();
@@ -363,8 +364,8 @@ __global__ void __launch_bounds__(256) k_batch(BatchDev b, int redo)
                     pending = true;
                 }
             }
-            double fp = pot_force<POT_CUSPY>(s, w, up);
-            double ff = scale(FQ_SUB(uf, up), skf);
+            double fp = pot_force<POT_CUSPY, SOFT>(s, w, up);
+            double ff = scale(S_SUB(4, uf, up), skf);
             int li2 = threadIdx.x * PPT + q;
             double uL = li2 > 0 ? sh_un[li2 - 1]
                                 : (l == 0 ? FQ_ADD(FQ_ADD(u0[off + n - 1], FQ_MUL(s.dt, v0[off + n - 1])),
@@ -378,17 +379,17 @@ __global__ void __launch_bounds__(256) k_batch(BatchDev b, int redo)
                 int64_t gr = l + 1 == n ? off : g + 1;
                 uR = FQ_ADD(FQ_ADD(u0[gr], FQ_MUL(s.dt, v0[gr])), FQ_MUL(s.hdt2, a0[gr]));
             }
-            double fi = scale(FQ_ADD(FQ_SUB(uL, scale_pow2(up, 1, 2.0)), uR), s.s_k);
-            double sfi = FQ_ADD(FQ_ADD(ff, fp), fi);
-            double v = FQ_ADD(vr[q], FQ_MUL(s.dt, ar[q]));
-            double f = FQ_ADD(sfi, FQ_MUL(s.me, v));
+            double fi = scale(S_ADD(8, S_SUB(7, uL, scale_pow2(up, 1, 2.0)), uR), s.s_k);
+            double sfi = S_ADD(9, S_ADD(6, ff, fp), fi);
+            double v = S_ADD(11, vr[q], S_MUL(10, s.dt, ar[q]));
+            double f = S_ADD(13, sfi, S_MUL(12, s.me, v));
             double a = scale(f, s.s_im);
-#pragma unroll
-            for (int rep = 0; rep < 2; ++rep) {
-                v = FQ_ADD(vr[q], FQ_MUL(s.hdt, FQ_ADD(ar[q], a)));
-                f = FQ_ADD(sfi, FQ_MUL(s.me, v));
-                a = scale(f, s.s_im);
-            }
+            v = S_ADD(16, vr[q], S_MUL(15, s.hdt, S_ADD(14, ar[q], a)));
+            f = S_ADD(18, sfi, S_MUL(17, s.me, v));
+            a = scale(f, s.s_im);
+            v = S_ADD(21, vr[q], S_MUL(20, s.hdt, S_ADD(19, ar[q], a)));
+            f = S_ADD(23, sfi, S_MUL(22, s.me, v));
+            a = scale(f, s.s_im);
             u1[g] = up;
             v1[g] = v;
             a1[g] = a;

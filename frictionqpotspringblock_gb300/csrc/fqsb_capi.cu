@@ -54,6 +54,8 @@ struct fqsb_system {
     cudaGraphExec_t graph;
     int graph_k;
     bool use_graph; /* false when FQSB_NO_GRAPH=1: host-driven launches (profiling) */
+    SmallGeom sg;   /* one-cluster run kernel of small systems */
+    bool small_ok;  /* N fits one cluster, 1d ring or no interactions, not disabled by FQSB_NO_SMALL=1 */
     std::string err;
     /* adjoint tape */
     int64_t adj_T, adj_K, adj_last, adj_nseg;
@@ -598,9 +600,13 @@ static int run(fqsb_system* h, int64_t max_steps, int flags, double tol, int64_t
             h->graph = nullptr;
         }
     }
-    rc = ensure_graph(h);
-    if (rc) {
-        return rc;
+    const bool use_small = h->small_ok && io == nullptr && !(flags & (RF_SCHEDULE | RF_RECORD | RF_FFSUM)) &&
+                           !((flags & RF_RESID) && niter_tol > SMALL_RING_MAX);
+    if (!use_small) {
+        rc = ensure_graph(h);
+        if (rc) {
+            return rc;
+        }
     }
     Ctl* c = h->h_ctl;
     memset(c, 0, sizeof(Ctl));
@@ -650,7 +656,10 @@ static int run(fqsb_system* h, int64_t max_steps, int flags, double tol, int64_t
         CU(h, cudaGetLastError());
     }
     for (;;) {
-        if (h->use_graph) {
+        if (use_small) {
+            CU(h, launch_small_run(h->d, h->sg, h->stream));
+        }
+        else if (h->use_graph) {
             CU(h, cudaGraphLaunch(h->graph, h->stream));
         }
         else {
@@ -848,8 +857,20 @@ extern "C" int fqsb_create(const fqsb_config* cfg, fqsb_system** out)
     d.s_kf = classify_scale(d.k_frame);
     d.s_im = classify_scale(d.inv_m);
     h->lg = line_geometry(N);
+    {
+        /* small Line1d / Particles systems: whole runs in one thread-block cluster */
+        const char* ns = getenv("FQSB_NO_SMALL");
+        const char* nc = getenv("FQSB_SMALL_CTAS");
+        int max_ctas = nc ? atoi(nc) : SMALL_MAX_CTAS;
+        h->sg = small_geometry(N, max_ctas);
+        if (h->sg.ok && h->sg.ctas > 8 && !small_cluster_fits(d, h->sg)) {
+            h->sg = small_geometry(N, 8); /* the GPU cannot co-schedule a cluster of 16 */
+        }
+        h->small_ok = h->sg.ok && cfg->interactions != FQSB_LAPLACE2D && !(ns && ns[0] == '1');
+    }
     int64_t nsteps_cta = step_ctas(d, h->lg);
     int64_t npart = h->is2d ? std::max(grid_reduce_ctas(N), nsteps_cta) : h->lg.grid;
+    npart = std::max(npart, (int64_t)SMALL_MAX_CTAS); /* the one-cluster run kernel's CTA subtrees */
     d.npartials = npart;
 
 #define ALLOC(ptr, bytes)                                                                                \

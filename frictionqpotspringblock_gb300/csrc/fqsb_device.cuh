@@ -28,6 +28,7 @@
 #include <stdint.h>
 
 #include "fq_math.h"
+#include "fq_soft64.h"
 
 namespace fqsb {
 
@@ -566,6 +567,42 @@ __device__ __forceinline__ bool in_well(double yl, double yr, double u)
     return dkey(yl) <= k && k < dkey(yr);
 }
 
+/*
+ * Per-operation choice of unit.  Bit i of SOFT set: operation site i of the particle update runs on
+ * the integer pipes (fq_soft64.h, bit-identical to the hardware instruction); clear: on the fp64
+ * pipe.  Sites: 0 dt*v, 1 hdt2*a, 2 u+dt*v, 3 +hdt2*a (position); 4 u_frame-u', 5 c-u' (Cuspy),
+ * 6 f_frame+f_pot, 7 uL-2u', 8 +uR, 9 +f_int (forces); 10 dt*a0, 11 v0+dt*a0, 12 -eta*v, 13 s+(-eta*v)
+ * (first velocity update); 14 a0+a, 15 hdt*(a0+a), 16 v0+hdt*(..), 17 -eta*v, 18 s+(-eta*v) (second)
+ * and 19..23 the same for the third.
+ */
+#define S_ADD(bit, a, b) (((SOFT >> (bit)) & 1u) ? fq_sadd((a), (b)) : FQ_ADD((a), (b)))
+#define S_SUB(bit, a, b) (((SOFT >> (bit)) & 1u) ? fq_ssub((a), (b)) : FQ_SUB((a), (b)))
+#define S_MUL(bit, a, b) (((SOFT >> (bit)) & 1u) ? fq_smul((a), (b)) : FQ_MUL((a), (b)))
+
+/*
+ * The split the step kernels use: all eight multiplications and the two additions of the position
+ * update on the integer pipes, the other fourteen additions on the fp64 pipe.  Measured on the
+ * N = 2^22 flow workload against other splits (all multiplications only; also the velocity or the
+ * force additions): 20.2 G particle-steps/s against 19.2-20.2 for the others and 14.8 with none.
+ */
+constexpr unsigned STEP_SOFT = (1u << 0) | (1u << 1) | (1u << 2) | (1u << 3) | (1u << 10) | (1u << 12) | (1u << 15) |
+                               (1u << 17) | (1u << 20) | (1u << 22);
+
+/* fp64 add / mul for work inside a run-time branch (residual and frame-force sums): volatile, so the
+ * compiler cannot execute them speculatively before the branch, as it does with the plain forms. */
+__device__ __forceinline__ double add_nospec(double a, double b)
+{
+    double r;
+    asm volatile("add.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(a), "d"(b));
+    return r;
+}
+__device__ __forceinline__ double mul_nospec(double a, double b)
+{
+    double r;
+    asm volatile("mul.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(a), "d"(b));
+    return r;
+}
+
 __device__ __forceinline__ bool is_nan_bits(double x)
 {
     return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
@@ -600,11 +637,11 @@ __device__ __forceinline__ double scale(double x, const Scale& sc)
 }
 
 /* Potential force, Cuspy detail.h:139-170 / SemiSmooth :236-277 / Smooth :379-409. */
-template <int POT>
+template <int POT, unsigned SOFT = 0u>
 __device__ __forceinline__ double pot_force(const DevSys& s, const double4_32a& w, double up)
 {
     if (POT == POT_CUSPY) {
-        return scale(FQ_SUB(w.z, up), s.s_mu);
+        return scale((SOFT >> 5) & 1u ? fq_ssub(w.z, up) : FQ_SUB(w.z, up), s.s_mu);
     }
     else if (POT == POT_SEMISMOOTH) {
         if (up < w.z) {
@@ -654,6 +691,41 @@ __device__ __forceinline__ double cta_tree(double x, double* sh)
         x = y;
     }
     return x;
+}
+
+/* Two cta_tree sums at once (one pair of barriers; the shuffles of x and y interleave).  Same trees,
+ * same results as cta_tree(x) and cta_tree(y).  sh needs 2 * blockDim/32 doubles. */
+__device__ __forceinline__ double2 cta_tree2(double x, double y, double* sh)
+{
+#pragma unroll
+    for (int m = 1; m < 32; m <<= 1) {
+        double xo = __shfl_xor_sync(0xffffffffu, x, m);
+        double yo = __shfl_xor_sync(0xffffffffu, y, m);
+        x = (threadIdx.x & m) ? FQ_ADD(xo, x) : FQ_ADD(x, xo);
+        y = (threadIdx.x & m) ? FQ_ADD(yo, y) : FQ_ADD(y, yo);
+    }
+    int nw = blockDim.x >> 5;
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) {
+        sh[wid] = x;
+        sh[32 + wid] = y;
+    }
+    __syncthreads();
+    if (wid == 0) {
+        double a = lane < nw ? sh[lane] : 0.0;
+        double b = lane < nw ? sh[32 + lane] : 0.0;
+#pragma unroll
+        for (int m = 1; m < 32; m <<= 1) {
+            double ao = __shfl_xor_sync(0xffffffffu, a, m);
+            double bo = __shfl_xor_sync(0xffffffffu, b, m);
+            a = (threadIdx.x & m) ? FQ_ADD(ao, a) : FQ_ADD(a, ao);
+            b = (threadIdx.x & m) ? FQ_ADD(bo, b) : FQ_ADD(b, bo);
+        }
+        x = a;
+        y = b;
+    }
+    return make_double2(x, y);
 }
 
 /* Pairwise sum of v[lo .. lo+len) with len a power of two (binary-counter order == recursive tree). */

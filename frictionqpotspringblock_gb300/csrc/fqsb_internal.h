@@ -35,6 +35,20 @@ int64_t step_ctas(const DevSys& s, const LineGeom& g);
  * Writes the conditional handles into s (they are kernel arguments of the graph's nodes). */
 cudaError_t build_run_graph(DevSys& s, const LineGeom& g, cudaGraphExec_t* exec);
 
+/* Small Line1d / Particles systems: a whole run in one launch of one thread-block cluster. */
+static const int SMALL_MAX_CTAS = 16;   /* cluster size limit (above 8 needs the non-portable opt-in) */
+static const int SMALL_RING_MAX = 1024; /* StopList windows up to this length stay in shared memory */
+struct SmallGeom {
+    int threads; /* per CTA, power of two in [32, 256] */
+    int ppt;     /* particles per thread: 1, 2 or 4 */
+    int ctas;    /* CTAs of the cluster */
+    bool ok;     /* N fits: N <= max_ctas * 1024 */
+};
+SmallGeom small_geometry(int64_t N, int max_ctas);
+cudaError_t launch_small_run(const DevSys& s, const SmallGeom& g, cudaStream_t st);
+/* Whether a cluster of g.ctas CTAs of this kernel can be co-scheduled (sizes above 8 are opt-in). */
+bool small_cluster_fits(const DevSys& s, const SmallGeom& g);
+
 /* One loop iteration launched kernel by kernel by the host (s.in_graph must be 0). */
 cudaError_t launch_iteration(const DevSys& s, const LineGeom& g, cudaStream_t st);
 

@@ -38,36 +38,52 @@
  */
 #include "fqsb_internal.h"
 
+#include <cooperative_groups.h>
+#include <cstdlib>
+
 namespace fqsb {
 
+/*
+ * Resident CTAs of 256 threads per SM the step kernels are compiled for (register cap 48 at 5).  The
+ * integer-pipe operations are long dependent chains; occupancy hides them (4.9 G particle-steps/s
+ * slower at the 93-112 registers the compiler picks unbounded).  The Smooth potential's
+ * double-double sine needs more registers than the cap allows without spilling.
+ */
+template <int POT>
+struct StepOcc {
+    static constexpr int value = POT == POT_SMOOTH ? 2 : 5;
+};
+
+template <unsigned SOFT = 0u>
 __device__ __forceinline__ double u_next(const DevSys& s, const double* u0, const double* v0, const double* a0,
                                          int64_t q)
 {
-    return FQ_ADD(FQ_ADD(u0[q], FQ_MUL(s.dt, v0[q])), FQ_MUL(s.hdt2, a0[q]));
+    return S_ADD(3, S_ADD(2, u0[q], S_MUL(0, s.dt, v0[q])), S_MUL(1, s.hdt2, a0[q]));
 }
 
 /* velocity / acceleration updates of timeStep after the positions, detail.h:1552-1565 */
+template <unsigned SOFT = 0u>
 __device__ __forceinline__ void verlet_velocity(const DevSys& s, double sfi, double v0, double a0, double& v, double& a,
                                                 double& f)
 {
-    v = FQ_ADD(v0, FQ_MUL(s.dt, a0));
-    f = FQ_ADD(sfi, FQ_MUL(s.me, v));
+    v = S_ADD(11, v0, S_MUL(10, s.dt, a0));
+    f = S_ADD(13, sfi, S_MUL(12, s.me, v));
     a = scale(f, s.s_im);
-#pragma unroll
-    for (int rep = 0; rep < 2; ++rep) {
-        v = FQ_ADD(v0, FQ_MUL(s.hdt, FQ_ADD(a0, a)));
-        f = FQ_ADD(sfi, FQ_MUL(s.me, v));
-        a = scale(f, s.s_im);
-    }
+    v = S_ADD(16, v0, S_MUL(15, s.hdt, S_ADD(14, a0, a)));
+    f = S_ADD(18, sfi, S_MUL(17, s.me, v));
+    a = scale(f, s.s_im);
+    v = S_ADD(21, v0, S_MUL(20, s.hdt, S_ADD(19, a0, a)));
+    f = S_ADD(23, sfi, S_MUL(22, s.me, v));
+    a = scale(f, s.s_im);
 }
 
 /* (f_frame + f_potential) of the force sum, and f_frame itself */
-template <int POT>
+template <int POT, unsigned SOFT = 0u>
 __device__ __forceinline__ double frame_pot(const DevSys& s, const double4_32a& w, double up, double uf, double& ff)
 {
-    double fp = pot_force<POT>(s, w, up);
-    ff = scale(FQ_SUB(uf, up), s.s_kf);
-    return FQ_ADD(ff, fp);
+    double fp = pot_force<POT, SOFT>(s, w, up);
+    ff = scale(S_SUB(4, uf, up), s.s_kf);
+    return S_ADD(6, ff, fp);
 }
 
 __device__ __forceinline__ long long absll(long long x)
@@ -97,12 +113,14 @@ __device__ __forceinline__ void set_branch(const DevSys& s, unsigned v)
 }
 
 /*
- * Stop tests of one finished step (thread 0 of the CTA that finishes the step last); sets the
- * run-loop condition.  sf / sff: sum of f^2 and of f_frame^2 over all particles.
+ * Bookkeeping and stop tests of one finished step on a run-control block c (global memory for the
+ * graph path, shared memory for the one-cluster path) and its StopList window `ring`: step and
+ * increment counters, frame position, plastic activity, NaN / yield-search errors, the StopList
+ * residual test (GooseFEM::Iterate::StopList, detail.h:1780-1783), event, truncation and step limits.
  */
-__device__ void finalize_step(const DevSys& s, double uf, double sf, double sff)
+template <typename CTL>
+__device__ __forceinline__ void finalize_ctl(CTL* c, double* ring, double uf, double sf, double sff)
 {
-    Ctl* c = s.ctl;
     int flags = c->flags;
     c->ticket = 0;
     c->ticket_redo = 0;
@@ -153,7 +171,6 @@ __device__ void finalize_step(const DevSys& s, double uf, double sf, double sff)
             c->last_residual = r;
             int64_t n = c->niter_tol;
             if (n > 0) {
-                double* ring = s.ring;
                 int64_t pos = c->sl_pos;
                 double old = ring[pos];
                 if (old >= c->tol) {
@@ -195,7 +212,17 @@ __device__ void finalize_step(const DevSys& s, double uf, double sf, double sff)
             c->done = RUN_MAXITER;
         }
     }
-    bool more = !c->done && !c->error && (now - c->launch_t0) < c->budget_ns;
+}
+
+/*
+ * Stop tests of one finished step (thread 0 of the CTA that finishes the step last); sets the
+ * run-loop condition.  sf / sff: sum of f^2 and of f_frame^2 over all particles.
+ */
+__device__ void finalize_step(const DevSys& s, double uf, double sf, double sff)
+{
+    Ctl* c = s.ctl;
+    finalize_ctl(c, s.ring, uf, sf, sff);
+    bool more = !c->done && !c->error && (globaltimer() - c->launch_t0) < c->budget_ns;
     __threadfence();
     set_loop(s, more ? 1u : 0u);
 }
@@ -422,11 +449,11 @@ __device__ __forceinline__ void step_epilogue(const DevSys& s, StepShared& sh, i
  * from the old state.  State arrays are padded to a multiple of 1024 entries.  redo = 1: only CTAs
  * marked pending run (after k_regen moved their particles' windows).
  */
-template <int POT, int INTER, int PPT>
-__global__ void __launch_bounds__(256) k_step_line(DevSys s, int redo)
+template <int POT, int INTER, int PPT, unsigned SOFT = STEP_SOFT, bool SHFL = false>
+__global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_line(DevSys s, int redo)
 {
     __shared__ StepShared sh;
-    __shared__ double sh_un[256 * PPT];
+    __shared__ double sh_un[SHFL ? 1 : 256 * PPT];
     if (!step_prologue(s, sh, true)) {
         return;
     }
@@ -466,23 +493,31 @@ __global__ void __launch_bounds__(256) k_step_line(DevSys s, int redo)
         vr[PPT - 1] = vv.y;
         ar[0] = aa.x;
         ar[PPT - 1] = aa.y;
-        un[0] = FQ_ADD(FQ_ADD(uu.x, FQ_MUL(s.dt, vr[0])), FQ_MUL(s.hdt2, ar[0]));
-        un[PPT - 1] = FQ_ADD(FQ_ADD(uu.y, FQ_MUL(s.dt, vr[PPT - 1])), FQ_MUL(s.hdt2, ar[PPT - 1]));
+        un[0] = S_ADD(3, S_ADD(2, uu.x, S_MUL(0, s.dt, vr[0])), S_MUL(1, s.hdt2, ar[0]));
+        un[PPT - 1] = S_ADD(3, S_ADD(2, uu.y, S_MUL(0, s.dt, vr[PPT - 1])), S_MUL(1, s.hdt2, ar[PPT - 1]));
     }
     else {
 #pragma unroll
         for (int j = 0; j < PPT; ++j) {
             vr[j] = v0[p0 + j];
             ar[j] = a0[p0 + j];
-            un[j] = FQ_ADD(FQ_ADD(u0[p0 + j], FQ_MUL(s.dt, vr[j])), FQ_MUL(s.hdt2, ar[j]));
+            un[j] = S_ADD(3, S_ADD(2, u0[p0 + j], S_MUL(0, s.dt, vr[j])), S_MUL(1, s.hdt2, ar[j]));
         }
     }
-    if (INTER == INTER_LAPLACE1D) {
+    if (INTER == INTER_LAPLACE1D && !SHFL) {
 #pragma unroll
         for (int j = 0; j < PPT; ++j) {
             sh_un[threadIdx.x * PPT + j] = un[j];
         }
         __syncthreads();
+    }
+    /* SHFL: neighbours' new positions from the adjacent lanes; the warp's two edge particles'
+     * neighbours are recomputed from the old state (no CTA barrier) */
+    const int lane = threadIdx.x & 31;
+    double fromL = 0.0, fromR = 0.0;
+    if (INTER == INTER_LAPLACE1D && SHFL) {
+        fromL = __shfl_up_sync(0xffffffffu, un[PPT - 1], 1);
+        fromR = __shfl_down_sync(0xffffffffu, un[0], 1);
     }
     double rf = 0.0, rff = 0.0;
     bool nan = false, pending = false;
@@ -500,31 +535,49 @@ __global__ void __launch_bounds__(256) k_step_line(DevSys s, int redo)
         double4_32a w = well_of(s, p, up, act, sh, regen);
         pending |= regen;
         double ff;
-        double sfp = frame_pot<POT>(s, w, up, uf, ff);
+        double sfp = frame_pot<POT, SOFT>(s, w, up, uf, ff);
         double fi = 0.0;
         if (INTER == INTER_LAPLACE1D) {
-            int li = threadIdx.x * PPT + j;
-            double uL = li > 0 ? sh_un[li - 1] : u_next(s, u0, v0, a0, p == 0 ? N - 1 : p - 1);
-            double uR = (li + 1 < T * PPT && p + 1 < N) ? sh_un[li + 1] : u_next(s, u0, v0, a0, p + 1 == N ? 0 : p + 1);
-            fi = scale(FQ_ADD(FQ_SUB(uL, scale_pow2(up, 1, 2.0)), uR), s.s_k);
+            double uL, uR;
+            if (SHFL) {
+                if (j > 0) {
+                    uL = un[j > 0 ? j - 1 : 0];
+                }
+                else {
+                    uL = lane > 0 ? fromL : u_next<SOFT>(s, u0, v0, a0, p == 0 ? N - 1 : p - 1);
+                }
+                if (j < PPT - 1 && p + 1 < N) {
+                    uR = un[j < PPT - 1 ? j + 1 : 0];
+                }
+                else {
+                    uR = (j == PPT - 1 && lane < 31 && p + 1 < N) ? fromR
+                                                                  : u_next<SOFT>(s, u0, v0, a0, p + 1 == N ? 0 : p + 1);
+                }
+            }
+            else {
+                int li = threadIdx.x * PPT + j;
+                uL = li > 0 ? sh_un[li - 1] : u_next(s, u0, v0, a0, p == 0 ? N - 1 : p - 1);
+                uR = (li + 1 < T * PPT && p + 1 < N) ? sh_un[li + 1] : u_next(s, u0, v0, a0, p + 1 == N ? 0 : p + 1);
+            }
+            fi = scale(S_ADD(8, S_SUB(7, uL, scale_pow2(up, 1, 2.0)), uR), s.s_k);
         }
-        double sfi = FQ_ADD(sfp, fi);
+        double sfi = S_ADD(9, sfp, fi);
         double f;
-        verlet_velocity(s, sfi, vr[j], ar[j], vo[j], ao[j], f);
+        verlet_velocity<SOFT>(s, sfi, vr[j], ar[j], vo[j], ao[j], f);
         nan |= is_nan_bits(up);
         if (resid) {
-            double f2 = FQ_MUL(f, f), ff2 = FQ_MUL(ff, ff);
+            double f2 = mul_nospec(f, f), ff2 = mul_nospec(ff, ff);
             if (j == 0) {
                 rf = f2;
                 rff = ff2;
             }
             else {
-                rf = FQ_ADD(rf, f2);
-                rff = FQ_ADD(rff, ff2);
+                rf = add_nospec(rf, f2);
+                rff = add_nospec(rff, ff2);
             }
         }
         else if (ffsum) {
-            rf = j == 0 ? ff : FQ_ADD(rf, ff);
+            rf = j == 0 ? ff : add_nospec(rf, ff);
         }
         if (record) {
             size_t o = (size_t)rec_step * (size_t)N + (size_t)p;
@@ -578,8 +631,8 @@ __global__ void __launch_bounds__(256) k_step_line(DevSys s, int redo)
  * written per particle (sq2) and summed in the flat-index pairwise order by k_reduce_grid, which
  * also finalises the step.
  */
-template <int POT>
-__global__ void __launch_bounds__(256) k_step_grid(DevSys s, int redo)
+template <int POT, unsigned SOFT = STEP_SOFT>
+__global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_grid(DevSys s, int redo)
 {
     __shared__ StepShared sh;
     __shared__ double sh_un[8][32];
@@ -613,7 +666,7 @@ __global__ void __launch_bounds__(256) k_step_grid(DevSys s, int redo)
     if (valid) {
         vr = v0[p];
         ar = a0[p];
-        up = FQ_ADD(FQ_ADD(u0[p], FQ_MUL(s.dt, vr)), FQ_MUL(s.hdt2, ar));
+        up = S_ADD(3, S_ADD(2, u0[p], S_MUL(0, s.dt, vr)), S_MUL(1, s.hdt2, ar));
         sh_un[ty][tx] = up;
     }
     __syncthreads();
@@ -631,15 +684,15 @@ __global__ void __launch_bounds__(256) k_step_grid(DevSys s, int redo)
             }
         }
         double ff;
-        double sfp = frame_pot<POT>(s, w, up, uf, ff);
+        double sfp = frame_pot<POT, SOFT>(s, w, up, uf, ff);
         double uU = ty > 0 ? sh_un[ty - 1][tx] : u_next(s, u0, v0, a0, ((i + R - 1) % R) * C + jc);
         double uD = (ty < 7 && i + 1 < R) ? sh_un[ty + 1][tx] : u_next(s, u0, v0, a0, ((i + 1) % R) * C + jc);
         double uL = tx > 0 ? sh_un[ty][tx - 1] : u_next(s, u0, v0, a0, i * C + (jc + C - 1) % C);
         double uR = (tx < 31 && jc + 1 < C) ? sh_un[ty][tx + 1] : u_next(s, u0, v0, a0, i * C + (jc + 1) % C);
         double fi = scale(FQ_SUB(FQ_ADD(FQ_ADD(FQ_ADD(uU, uD), uL), uR), scale_pow2(up, 2, 4.0)), s.s_k);
-        double sfi = FQ_ADD(sfp, fi);
+        double sfi = S_ADD(9, sfp, fi);
         double vv, aa, f;
-        verlet_velocity(s, sfi, vr, ar, vv, aa, f);
+        verlet_velocity<SOFT>(s, sfi, vr, ar, vv, aa, f);
         s.u[cur ^ 1][p] = up;
         s.v[cur ^ 1][p] = vv;
         s.a[cur ^ 1][p] = aa;
@@ -647,7 +700,7 @@ __global__ void __launch_bounds__(256) k_step_grid(DevSys s, int redo)
             sh.nan = 1;
         }
         if (resid) {
-            s.sq2[p] = make_double2(FQ_MUL(f, f), FQ_MUL(ff, ff));
+            s.sq2[p] = make_double2(mul_nospec(f, f), mul_nospec(ff, ff));
         }
     }
     if (redo) {
@@ -725,6 +778,331 @@ __global__ void __launch_bounds__(128) k_regen(DevSys s)
     }
 }
 
+/* ------------------------------------------------------------- small systems: one cluster */
+
+/*
+ * A whole run of a small Line1d / Particles system in one launch of one thread-block cluster (up to
+ * 8 CTAs on 8 SMs).  For small N the graph path is bound by its per-step launch and node overhead
+ * (about 20 us per time step at N = 1024, no faster than one CPU core); here the state stays in
+ * registers for the whole run, the new positions at tile edges cross CTA boundaries through
+ * distributed shared memory, and cluster barriers replace the per-step launches.  Per time step:
+ *   position update -> barrier A -> wells, forces, velocities, CTA residual subtree -> barrier B ->
+ *   CTA 0 sums the subtrees and runs the same stop tests as the graph path (finalize_step) ->
+ *   barrier C -> every CTA reads the decision.
+ * Arithmetic, the residual tree (aligned power-of-two tiles) and the finalisation are those of
+ * k_step_line, and chunk windows are moved inline (dev_align, as k_regen does), so the results equal
+ * the graph path's bit for bit.  Runs that record a trajectory (adjoint) use the graph path.
+ */
+template <int POT, int INTER, int PPT>
+__global__ void __launch_bounds__(256) k_run_small(DevSys s)
+{
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    __shared__ double sh_un[2][256 * PPT];
+    __shared__ double red[64];
+    /* CTA 0 keeps the run-control block, the StopList window and the CTA subtrees of the residual */
+    __shared__ Ctl sc;
+    __shared__ double sring[SMALL_RING_MAX];
+    __shared__ double2 spart[SMALL_MAX_CTAS];
+    __shared__ int sh_exit;
+    __shared__ int sh_nan, sh_walk;
+    __shared__ unsigned long long sh_ds, sh_da;
+
+    const unsigned rank = cluster.block_rank();
+    const unsigned G = cluster.num_blocks();
+    const int tid = threadIdx.x;
+    const int64_t N = s.N;
+    const int64_t tile = (int64_t)blockDim.x * PPT;
+    const int64_t base = (int64_t)rank * tile;
+    const int64_t p0 = base + (int64_t)tid * PPT;
+    const Ctl* gc = s.ctl;
+    const int flags = gc->flags;
+    const bool act = (flags & (RF_ACT | RF_TRUNCATE | RF_EVENT)) != 0;
+    const bool resid = (flags & RF_RESID) != 0;
+    const double vdt = gc->vdt;
+    double uf = gc->u_frame;
+    int cur = gc->cur;
+    const int64_t nring = (resid && gc->niter_tol > 0) ? gc->niter_tol : 0;
+    if (rank == 0) {
+        if (tid == 0) {
+            sc = *gc;
+        }
+        for (int64_t i = tid; i < nring; i += blockDim.x) {
+            sring[i] = s.ring[i];
+        }
+    }
+
+    /* ring neighbours of the tile's first and last particle: (CTA rank, index in its tile) */
+    const int64_t plast = (base + tile < N ? base + tile : N) - 1;
+    const int64_t pl = base == 0 ? N - 1 : base - 1;
+    const int64_t pr = plast + 1 == N ? 0 : plast + 1;
+    const int il = (int)(pl % tile), ir = (int)(pr % tile);
+    const double* left[2] = {cluster.map_shared_rank(&sh_un[0][0], (unsigned)(pl / tile)),
+                             cluster.map_shared_rank(&sh_un[1][0], (unsigned)(pl / tile))};
+    const double* right[2] = {cluster.map_shared_rank(&sh_un[0][0], (unsigned)(pr / tile)),
+                              cluster.map_shared_rank(&sh_un[1][0], (unsigned)(pr / tile))};
+    Ctl* sc0 = cluster.map_shared_rank(&sc, 0);
+    double2* spart0 = cluster.map_shared_rank(&spart[0], 0);
+    const int* exit0 = cluster.map_shared_rank(&sh_exit, 0);
+
+    double u[PPT], v[PPT], a[PPT];
+    double4_32a w[PPT];
+#pragma unroll
+    for (int j = 0; j < PPT; ++j) {
+        int64_t p = p0 + j;
+        if (p < N) {
+            u[j] = s.u[cur][p];
+            v[j] = s.v[cur][p];
+            a[j] = s.a[cur][p];
+            w[j] = s.wc[p];
+        }
+        else {
+            u[j] = v[j] = a[j] = 0.0;
+            w[j] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
+        }
+    }
+    /* one particle per thread: latency bound, all fp64 on the fp64 pipe; more: throughput bound, split */
+    constexpr unsigned SOFT = PPT >= 2 ? STEP_SOFT : 0u;
+    int buf = 0;
+    bool first = true;
+    for (;;) {
+        const double uf_prev = uf;
+        if (flags & RF_FLOW) {
+            uf = FQ_ADD(uf, vdt);
+        }
+        double un[PPT];
+#pragma unroll
+        for (int j = 0; j < PPT; ++j) {
+            un[j] = S_ADD(3, S_ADD(2, u[j], S_MUL(0, s.dt, v[j])), S_MUL(1, s.hdt2, a[j]));
+            sh_un[buf][tid * PPT + j] = un[j];
+        }
+        if (tid == 0) {
+            sh_ds = 0ull;
+            sh_da = 0ull;
+            sh_nan = 0;
+            sh_walk = 0;
+        }
+        /* A: every tile's new positions, and CTA 0's decision on the previous step (at the start: its
+         * control block).  On a stop the positions just computed are dropped. */
+        cluster.sync();
+        if (!first && *exit0) {
+            uf = uf_prev;
+            break;
+        }
+        first = false;
+        double rf = 0.0, rff = 0.0;
+        bool nan = false;
+#pragma unroll
+        for (int j = 0; j < PPT; ++j) {
+            int64_t p = p0 + j;
+            if (p >= N) {
+                continue;
+            }
+            double up = un[j];
+            double4_32a ww = w[j];
+            if (!in_well(ww.x, ww.y, up) && !non_finite(up)) {
+                int64_t gold = s.gidx[p];
+                if (!window_search(s, p, up, ww)) {
+                    dev_align(s, p, up); /* moves the chunk window; a failed search sets walk_flag */
+                    ww = s.wc[p];
+                    if (((volatile Ctl*)s.ctl)->walk_flag) {
+                        sh_walk = 1;
+                    }
+                }
+                int64_t gnew = s.gidx[p];
+                if (act && gnew != gold) {
+                    int64_t ref = s.i_n[p];
+                    long long ds = absll(gnew - ref) - absll(gold - ref);
+                    long long da = (long long)(gnew != ref) - (long long)(gold != ref);
+                    atomicAdd(&sh_ds, (unsigned long long)ds);
+                    atomicAdd(&sh_da, (unsigned long long)da);
+                }
+                w[j] = ww;
+            }
+            double ff;
+            double sfp = frame_pot<POT, SOFT>(s, ww, up, uf, ff);
+            double fi = 0.0;
+            if (INTER == INTER_LAPLACE1D) {
+                int li = tid * PPT + j;
+                double uL = li > 0 ? sh_un[buf][li - 1] : left[buf][il];
+                double uR = (li + 1 < tile && p + 1 < N) ? sh_un[buf][li + 1] : right[buf][ir];
+                fi = scale(S_ADD(8, S_SUB(7, uL, scale_pow2(up, 1, 2.0)), uR), s.s_k);
+            }
+            double sfi = S_ADD(9, sfp, fi);
+            double vn, an, f;
+            verlet_velocity<SOFT>(s, sfi, v[j], a[j], vn, an, f);
+            u[j] = up;
+            v[j] = vn;
+            a[j] = an;
+            nan |= is_nan_bits(up);
+            if (resid) {
+                double f2 = mul_nospec(f, f), ff2 = mul_nospec(ff, ff);
+                if (j == 0) {
+                    rf = f2;
+                    rff = ff2;
+                }
+                else {
+                    rf = add_nospec(rf, f2);
+                    rff = add_nospec(rff, ff2);
+                }
+            }
+        }
+        if (nan) {
+            sh_nan = 1;
+        }
+        double2 sfs = make_double2(0.0, 0.0);
+        if (resid) {
+            sfs = cta_tree2(rf, rff, red);
+        }
+        __syncthreads();
+        if (tid == 0) {
+            if (resid) {
+                spart0[rank] = sfs;
+            }
+            if (sh_ds) {
+                atomicAdd((unsigned long long*)&sc0->s_sum, sh_ds);
+            }
+            if (sh_da) {
+                atomicAdd((unsigned long long*)&sc0->a_count, sh_da);
+            }
+            if (sh_nan) {
+                atomicOr(&sc0->nan_flag, 1);
+            }
+            if (sh_walk) {
+                atomicOr(&sc0->walk_flag, 1);
+            }
+        }
+        cluster.sync(); /* B: every tile's residual subtree and counters */
+        if (rank == 0 && tid < 32) {
+            double tx = 0.0, ty = 0.0;
+            if (resid) {
+                /* the canonical tree over the CTA subtrees, zero padded (as tree_partials): G <= 32 */
+                double x = 0.0, y = 0.0;
+                if ((unsigned)tid < G) {
+                    x = spart[tid].x;
+                    y = spart[tid].y;
+                }
+                tx = warp_tree(x);
+                ty = warp_tree(y);
+            }
+            if (tid == 0) {
+                finalize_ctl(&sc, sring, uf, tx, ty);
+                sh_exit = (sc.done || sc.error || (globaltimer() - sc.launch_t0) >= sc.budget_ns) ? 1 : 0;
+            }
+        }
+        buf ^= 1;
+    }
+    cur = sc0->cur;
+#pragma unroll
+    for (int j = 0; j < PPT; ++j) {
+        int64_t p = p0 + j;
+        if (p < N) {
+            s.u[cur][p] = u[j];
+            s.v[cur][p] = v[j];
+            s.a[cur][p] = a[j];
+        }
+    }
+    if (rank == 0) {
+        for (int64_t i = tid; i < nring; i += blockDim.x) {
+            s.ring[i] = sring[i];
+        }
+        if (tid == 0) {
+            *s.ctl = sc;
+        }
+    }
+    /* no CTA may exit while others still read its shared memory */
+    cluster.sync();
+}
+
+SmallGeom small_geometry(int64_t N, int max_ctas)
+{
+    SmallGeom g;
+    int64_t per = (N + max_ctas - 1) / max_ctas;
+    int64_t tile = 32;
+    while (tile < per) {
+        tile <<= 1;
+    }
+    g.threads = (int)(tile < 256 ? tile : 256);
+    g.ppt = (int)(tile / g.threads);
+    g.ctas = (int)((N + tile - 1) / tile);
+    g.ok = N >= 1 && tile <= 1024 && max_ctas <= SMALL_MAX_CTAS;
+    return g;
+}
+
+template <int POT, int INTER>
+static const void* small_kernel_t(int ppt)
+{
+    switch (ppt) {
+        case 1: return (const void*)k_run_small<POT, INTER, 1>;
+        case 2: return (const void*)k_run_small<POT, INTER, 2>;
+        default: return (const void*)k_run_small<POT, INTER, 4>;
+    }
+}
+
+static const void* small_kernel(const DevSys& s, const SmallGeom& g)
+{
+    if (s.inter == INTER_LAPLACE1D) {
+        return s.pot == POT_CUSPY ? small_kernel_t<POT_CUSPY, INTER_LAPLACE1D>(g.ppt)
+               : s.pot == POT_SEMISMOOTH ? small_kernel_t<POT_SEMISMOOTH, INTER_LAPLACE1D>(g.ppt)
+                                         : small_kernel_t<POT_SMOOTH, INTER_LAPLACE1D>(g.ppt);
+    }
+    return s.pot == POT_CUSPY ? small_kernel_t<POT_CUSPY, INTER_NONE>(g.ppt)
+           : s.pot == POT_SEMISMOOTH ? small_kernel_t<POT_SEMISMOOTH, INTER_NONE>(g.ppt)
+                                     : small_kernel_t<POT_SMOOTH, INTER_NONE>(g.ppt);
+}
+
+static void small_launch_config(const SmallGeom& g, cudaStream_t st, cudaLaunchConfig_t& cfg, cudaLaunchAttribute* attr)
+{
+    cfg = {};
+    cfg.gridDim = dim3((unsigned)g.ctas);
+    cfg.blockDim = dim3((unsigned)g.threads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)g.ctas;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+}
+
+bool small_cluster_fits(const DevSys& s, const SmallGeom& g)
+{
+    const void* f = small_kernel(s, g);
+    if (cudaFuncSetAttribute(f, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    cudaLaunchConfig_t cfg;
+    cudaLaunchAttribute attr[1];
+    small_launch_config(g, nullptr, cfg, attr);
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, f, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return n >= 1;
+}
+
+cudaError_t launch_small_run(const DevSys& s, const SmallGeom& g, cudaStream_t st)
+{
+    const void* f = small_kernel(s, g);
+    if (g.ctas > 8) {
+        /* clusters above the portable size of 8 must be allowed per kernel */
+        cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        if (e != cudaSuccess) {
+            return e;
+        }
+    }
+    cudaLaunchConfig_t cfg;
+    cudaLaunchAttribute attr[1];
+    small_launch_config(g, st, cfg, attr);
+    DevSys arg = s;
+    arg.in_graph = 0; /* not inside the run graph: no conditional handles to set */
+    void* args[] = {(void*)&arg};
+    return cudaLaunchKernelExC(&cfg, f, args);
+}
+
 /* ------------------------------------------------------------- geometry */
 
 LineGeom line_geometry(int64_t N)
@@ -759,6 +1137,11 @@ int64_t step_ctas(const DevSys& s, const LineGeom& g)
 template <int POT, int INTER>
 static void* line_kernel_t(int ppt)
 {
+    const char* v = getenv("FQSB_STEP_SHFL");
+    if (v && v[0] == '1') {
+        return ppt == 2 ? (void*)k_step_line<POT, INTER, 2, STEP_SOFT, true>
+                        : (void*)k_step_line<POT, INTER, 1, STEP_SOFT, true>;
+    }
     return ppt == 2 ? (void*)k_step_line<POT, INTER, 2> : (void*)k_step_line<POT, INTER, 1>;
 }
 

@@ -315,3 +315,16 @@ def test_regeneration_inside_steps_large():
     ref.flowSteps(800, 0.5)
     assert_same(gpu, ref)
     assert np.max(gpu.chunk.start) > 0
+
+
+def test_large_ring_two_per_thread():
+    """1d N = 2^18: the launch shape with two particles per thread (N >= 2 * 152 * 512), the one the
+    large-N throughput workload runs; flow with window regeneration, a frame jump and minimise."""
+    gpu, ref = make_pair("Line1d_Cuspy", [2 ** 18], nchunk=40, offset=-5.0)
+    gpu.flowSteps(400, 0.5)
+    ref.flowSteps(400, 0.5)
+    assert_same(gpu, ref)
+    gpu.u_frame = gpu.u_frame + 0.5
+    ref.u_frame = ref.u_frame + 0.5
+    assert gpu.minimise(max_iter=3000, max_iter_is_error=False) == ref.minimise(max_iter=3000, max_iter_is_error=False)
+    assert_same(gpu, ref)
