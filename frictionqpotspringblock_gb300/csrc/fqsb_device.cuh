@@ -661,13 +661,18 @@ __device__ __forceinline__ double pot_force(const DevSys& s, const double4_32a& 
 
 /* ------------------------------------------------ canonical reductions */
 
-/* Sum over the 32 lanes in the fixed pairwise order (lane i with i^1, then pairs of pairs, ...). */
+/* Sum over the 32 lanes in the fixed pairwise order (lane i with i+1, then pairs of pairs, ...), the
+ * result in lane 0.  At level m only the lanes that start a pair of width 2m add (the others' values
+ * are no longer needed); the add is non-speculatable so that the idle lanes do not issue it (the fp64
+ * pipe's cost follows the active lanes). */
 __device__ __forceinline__ double warp_tree(double x)
 {
 #pragma unroll
     for (int m = 1; m < 32; m <<= 1) {
-        double y = __shfl_xor_sync(0xffffffffu, x, m);
-        x = (threadIdx.x & m) ? FQ_ADD(y, x) : FQ_ADD(x, y);
+        double y = __shfl_down_sync(0xffffffffu, x, m);
+        if ((threadIdx.x & (2 * m - 1)) == 0) {
+            x = add_nospec(x, y);
+        }
     }
     return x;
 }
@@ -699,10 +704,12 @@ __device__ __forceinline__ double2 cta_tree2(double x, double y, double* sh)
 {
 #pragma unroll
     for (int m = 1; m < 32; m <<= 1) {
-        double xo = __shfl_xor_sync(0xffffffffu, x, m);
-        double yo = __shfl_xor_sync(0xffffffffu, y, m);
-        x = (threadIdx.x & m) ? FQ_ADD(xo, x) : FQ_ADD(x, xo);
-        y = (threadIdx.x & m) ? FQ_ADD(yo, y) : FQ_ADD(y, yo);
+        double xo = __shfl_down_sync(0xffffffffu, x, m);
+        double yo = __shfl_down_sync(0xffffffffu, y, m);
+        if ((threadIdx.x & (2 * m - 1)) == 0) {
+            x = add_nospec(x, xo);
+            y = add_nospec(y, yo);
+        }
     }
     int nw = blockDim.x >> 5;
     int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -717,10 +724,12 @@ __device__ __forceinline__ double2 cta_tree2(double x, double y, double* sh)
         double b = lane < nw ? sh[32 + lane] : 0.0;
 #pragma unroll
         for (int m = 1; m < 32; m <<= 1) {
-            double ao = __shfl_xor_sync(0xffffffffu, a, m);
-            double bo = __shfl_xor_sync(0xffffffffu, b, m);
-            a = (threadIdx.x & m) ? FQ_ADD(ao, a) : FQ_ADD(a, ao);
-            b = (threadIdx.x & m) ? FQ_ADD(bo, b) : FQ_ADD(b, bo);
+            double ao = __shfl_down_sync(0xffffffffu, a, m);
+            double bo = __shfl_down_sync(0xffffffffu, b, m);
+            if ((threadIdx.x & (2 * m - 1)) == 0) {
+                a = add_nospec(a, ao);
+                b = add_nospec(b, bo);
+            }
         }
         x = a;
         y = b;

@@ -39,7 +39,6 @@
 #include "fqsb_internal.h"
 
 #include <cooperative_groups.h>
-#include <cstdlib>
 
 namespace fqsb {
 
@@ -449,11 +448,11 @@ __device__ __forceinline__ void step_epilogue(const DevSys& s, StepShared& sh, i
  * from the old state.  State arrays are padded to a multiple of 1024 entries.  redo = 1: only CTAs
  * marked pending run (after k_regen moved their particles' windows).
  */
-template <int POT, int INTER, int PPT, unsigned SOFT = STEP_SOFT, bool SHFL = false>
+template <int POT, int INTER, int PPT, unsigned SOFT = STEP_SOFT>
 __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_line(DevSys s, int redo)
 {
     __shared__ StepShared sh;
-    __shared__ double sh_un[SHFL ? 1 : 256 * PPT];
+    __shared__ double sh_un[256 * PPT];
     if (!step_prologue(s, sh, true)) {
         return;
     }
@@ -504,20 +503,12 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_line(DevSys s
             un[j] = S_ADD(3, S_ADD(2, u0[p0 + j], S_MUL(0, s.dt, vr[j])), S_MUL(1, s.hdt2, ar[j]));
         }
     }
-    if (INTER == INTER_LAPLACE1D && !SHFL) {
+    if (INTER == INTER_LAPLACE1D) {
 #pragma unroll
         for (int j = 0; j < PPT; ++j) {
             sh_un[threadIdx.x * PPT + j] = un[j];
         }
         __syncthreads();
-    }
-    /* SHFL: neighbours' new positions from the adjacent lanes; the warp's two edge particles'
-     * neighbours are recomputed from the old state (no CTA barrier) */
-    const int lane = threadIdx.x & 31;
-    double fromL = 0.0, fromR = 0.0;
-    if (INTER == INTER_LAPLACE1D && SHFL) {
-        fromL = __shfl_up_sync(0xffffffffu, un[PPT - 1], 1);
-        fromR = __shfl_down_sync(0xffffffffu, un[0], 1);
     }
     double rf = 0.0, rff = 0.0;
     bool nan = false, pending = false;
@@ -538,27 +529,9 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_line(DevSys s
         double sfp = frame_pot<POT, SOFT>(s, w, up, uf, ff);
         double fi = 0.0;
         if (INTER == INTER_LAPLACE1D) {
-            double uL, uR;
-            if (SHFL) {
-                if (j > 0) {
-                    uL = un[j > 0 ? j - 1 : 0];
-                }
-                else {
-                    uL = lane > 0 ? fromL : u_next<SOFT>(s, u0, v0, a0, p == 0 ? N - 1 : p - 1);
-                }
-                if (j < PPT - 1 && p + 1 < N) {
-                    uR = un[j < PPT - 1 ? j + 1 : 0];
-                }
-                else {
-                    uR = (j == PPT - 1 && lane < 31 && p + 1 < N) ? fromR
-                                                                  : u_next<SOFT>(s, u0, v0, a0, p + 1 == N ? 0 : p + 1);
-                }
-            }
-            else {
-                int li = threadIdx.x * PPT + j;
-                uL = li > 0 ? sh_un[li - 1] : u_next(s, u0, v0, a0, p == 0 ? N - 1 : p - 1);
-                uR = (li + 1 < T * PPT && p + 1 < N) ? sh_un[li + 1] : u_next(s, u0, v0, a0, p + 1 == N ? 0 : p + 1);
-            }
+            int li = threadIdx.x * PPT + j;
+            double uL = li > 0 ? sh_un[li - 1] : u_next(s, u0, v0, a0, p == 0 ? N - 1 : p - 1);
+            double uR = (li + 1 < T * PPT && p + 1 < N) ? sh_un[li + 1] : u_next(s, u0, v0, a0, p + 1 == N ? 0 : p + 1);
             fi = scale(S_ADD(8, S_SUB(7, uL, scale_pow2(up, 1, 2.0)), uR), s.s_k);
         }
         double sfi = S_ADD(9, sfp, fi);
@@ -566,7 +539,8 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_line(DevSys s
         verlet_velocity<SOFT>(s, sfi, vr[j], ar[j], vo[j], ao[j], f);
         nan |= is_nan_bits(up);
         if (resid) {
-            double f2 = mul_nospec(f, f), ff2 = mul_nospec(ff, ff);
+            /* squares on the integer pipes (bit-identical), sums on the fp64 pipe */
+            double f2 = fq_smul(f, f), ff2 = fq_smul(ff, ff);
             if (j == 0) {
                 rf = f2;
                 rff = ff2;
@@ -1137,11 +1111,6 @@ int64_t step_ctas(const DevSys& s, const LineGeom& g)
 template <int POT, int INTER>
 static void* line_kernel_t(int ppt)
 {
-    const char* v = getenv("FQSB_STEP_SHFL");
-    if (v && v[0] == '1') {
-        return ppt == 2 ? (void*)k_step_line<POT, INTER, 2, STEP_SOFT, true>
-                        : (void*)k_step_line<POT, INTER, 1, STEP_SOFT, true>;
-    }
     return ppt == 2 ? (void*)k_step_line<POT, INTER, 2> : (void*)k_step_line<POT, INTER, 1>;
 }
 
