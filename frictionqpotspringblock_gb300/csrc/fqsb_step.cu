@@ -245,10 +245,7 @@ __device__ double2 tree_partials(const double2* partials, int64_t G, double* sh)
         x = serial_tree([&](int64_t i) { return i < G ? __ldcg(partials + i).x : 0.0; }, lo, per);
         y = serial_tree([&](int64_t i) { return i < G ? __ldcg(partials + i).y : 0.0; }, lo, per);
     }
-    double sx = cta_tree(x, sh);
-    __syncthreads();
-    double sy = cta_tree(y, sh);
-    return make_double2(sx, sy);
+    return cta_tree2(x, y, sh);
 }
 
 struct StepShared {
@@ -261,7 +258,7 @@ struct StepShared {
     double uf;
     unsigned long long ds;
     unsigned long long da;
-    double red[32];
+    double red[64];
 };
 
 /* Reads the run state; returns false when the run is already over (then CTA 0 ends the loop). */
@@ -378,9 +375,9 @@ __device__ __forceinline__ void step_epilogue(const DevSys& s, StepShared& sh, i
     const bool tree = resid && mode != EPI_GRID_STEP;
     double sf = 0.0, sff = 0.0;
     if (tree) {
-        sf = cta_tree(rf, sh.red);
-        __syncthreads();
-        sff = cta_tree(rff, sh.red);
+        double2 t = cta_tree2(rf, rff, sh.red);
+        sf = t.x;
+        sff = t.y;
     }
     __syncthreads();
     int tid = threadIdx.x + threadIdx.y * blockDim.x;
