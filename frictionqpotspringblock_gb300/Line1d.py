@@ -61,3 +61,43 @@ class System_Smooth_Laplace(System):
                  offset=-100.0, nchunk=5000, **kwargs):
         super().__init__(m, eta, mu, k_interactions, k_frame, dt, shape, seed, distribution, parameters,
                          offset=offset, nchunk=nchunk, **kwargs)
+
+
+class _Hidden:
+    """A member of the base class that this class does not have (raises AttributeError, hasattr is False)."""
+
+    def __set_name__(self, owner, name):
+        self._name = name
+
+    def __get__(self, obj, objtype=None):
+        raise AttributeError(f"'{objtype.__name__}' object has no attribute '{self._name}'")
+
+
+class System_Cuspy_Laplace_Nopassing(System):
+    """Cuspy + Laplace1d minimised with the no-passing rule, no dynamics (main.cpp:532-568, Line1d.h:173-238).
+
+    m = 1; minimise() runs the overdamped no-passing fixed point (detail.h:1694-1753); the time-stepping
+    members are absent as in the reference (its binding omits mySystemNdDynamics)."""
+
+    _potential = C.CUSPY
+    _interactions = C.LAPLACE1D
+    _rank = 1
+    _name = "Line1d.System_Cuspy_Laplace_Nopassing"
+
+    timeStep = _Hidden()
+    timeSteps = _Hidden()
+    timeStepsUntilEvent = _Hidden()
+    flowSteps = _Hidden()
+
+    def __init__(self, mu, k_interactions, k_frame, shape, seed, distribution, parameters, offset=-100.0,
+                 nchunk=5000, eta=0.0, dt=0.0, **kwargs):
+        super().__init__(1.0, eta, mu, k_interactions, k_frame, dt, shape, seed, distribution, parameters,
+                         offset=offset, nchunk=nchunk, **kwargs)
+
+    def minimise(self, tol=1e-5, niter_tol=10, max_iter=int(1e9), time_activity=False, max_iter_is_error=True) -> int:
+        if time_activity:
+            raise RuntimeError("assertion failed (!time_activity)")
+        out = C.ctypes.c_uint64()
+        C.check(self._h, C.lib().fqsb_minimise_nopassing(self._h, float(tol), int(niter_tol), int(max_iter),
+                                                          int(bool(max_iter_is_error)), C.ctypes.byref(out)))
+        return out.value

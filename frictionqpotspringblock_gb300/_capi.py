@@ -111,6 +111,7 @@ SIGNATURES = [
     ("fqsb_time_steps_until_event", _I, [_P, _D, _U64, _U64, _PU64]),
     ("fqsb_minimise", _I, [_P, _D, _U64, _U64, _I, _I, _PU64]),
     ("fqsb_minimise_truncate", _I, [_P, _PI64, _U64, _U64, _D, _U64, _U64, _I, _I, _PU64]),
+    ("fqsb_minimise_nopassing", _I, [_P, _D, _U64, _U64, _I, _PU64]),
     ("fqsb_max_uniform_displacement", _I, [_P, _I, _PD]),
     ("fqsb_event_driven_step", _I, [_P, _D, _I, _I, _PD]),
     ("fqsb_trigger", _I, [_P, _I64, _D, _I]),

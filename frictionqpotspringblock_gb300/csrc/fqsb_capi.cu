@@ -52,6 +52,7 @@ struct fqsb_system {
     Ctl* h_ctl;              /* pinned */
     int64_t ring_cap;
     cudaGraphExec_t graph;
+    cudaGraphExec_t graph_np; /* the no-passing minimiser's run graph */
     int graph_k;
     bool use_graph; /* false when FQSB_NO_GRAPH=1: host-driven launches (profiling) */
     SmallGeom sg;   /* one-cluster run kernel of small systems */
@@ -577,7 +578,7 @@ struct RunIO {
 
 static int run(fqsb_system* h, int64_t max_steps, int flags, double tol, int64_t niter_tol, double vdt,
                int64_t A_truncate, int64_t S_truncate, const int64_t* i_n_host, RunResult* res,
-               const RunIO* io = nullptr)
+               const RunIO* io = nullptr, const NopassArgs* np = nullptr)
 {
     res->done = RUN_MAXITER;
     res->error = 0;
@@ -599,10 +600,23 @@ static int run(fqsb_system* h, int64_t max_steps, int flags, double tol, int64_t
             cudaGraphExecDestroy(h->graph);
             h->graph = nullptr;
         }
+        if (h->graph_np) {
+            cudaGraphExecDestroy(h->graph_np);
+            h->graph_np = nullptr;
+        }
     }
-    const bool use_small = h->small_ok && io == nullptr && !(flags & (RF_SCHEDULE | RF_RECORD | RF_FFSUM)) &&
+    const bool use_small = np == nullptr && h->small_ok && io == nullptr &&
+                           !(flags & (RF_SCHEDULE | RF_RECORD | RF_FFSUM)) &&
                            !((flags & RF_RESID) && niter_tol > SMALL_RING_MAX);
-    if (!use_small) {
+    if (np) {
+        if (h->use_graph && !h->graph_np) {
+            CU(h, build_nopass_graph(h->d, h->lg, *np, &h->graph_np));
+        }
+        if (!h->use_graph) {
+            h->d.in_graph = 0;
+        }
+    }
+    else if (!use_small) {
         rc = ensure_graph(h);
         if (rc) {
             return rc;
@@ -656,7 +670,19 @@ static int run(fqsb_system* h, int64_t max_steps, int flags, double tol, int64_t
         CU(h, cudaGetLastError());
     }
     for (;;) {
-        if (use_small) {
+        if (np) {
+            if (h->use_graph) {
+                CU(h, cudaGraphLaunch(h->graph_np, h->stream));
+            }
+            else {
+                DevSys d = h->d;
+                d.in_graph = 0;
+                for (int i = 0; i < 64; ++i) {
+                    CU(h, launch_nopass_iteration(d, h->lg, *np, h->stream));
+                }
+            }
+        }
+        else if (use_small) {
             CU(h, launch_small_run(h->d, h->sg, h->stream));
         }
         else if (h->use_graph) {
@@ -741,6 +767,9 @@ static void free_all(fqsb_system* h)
     if (h->graph) {
         cudaGraphExecDestroy(h->graph);
     }
+    if (h->graph_np) {
+        cudaGraphExecDestroy(h->graph_np);
+    }
     if (h->h_ctl) {
         cudaFreeHost(h->h_ctl);
     }
@@ -796,6 +825,7 @@ extern "C" int fqsb_create(const fqsb_config* cfg, fqsb_system** out)
     h->h_ctl = nullptr;
     h->ring_cap = 0;
     h->graph = nullptr;
+    h->graph_np = nullptr;
     h->graph_k = 0;
     {
         const char* ng = getenv("FQSB_NO_GRAPH");
@@ -1091,6 +1121,72 @@ extern "C" int fqsb_minimise_truncate(fqsb_system* h, const int64_t* i_n, uint64
         return set_err(h, FQSB_ERR_INVALID, "assertion failed (time_activity)");
     }
     return minimise_common(h, i_n, A_truncate, S_truncate, tol, niter_tol, max_iter, 1, max_iter_is_error, true, ret);
+}
+
+__global__ void k_damping_only(DevSys d, const double* v, double* f_damp)
+{
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < d.N) {
+        f_damp[p] = FQ_MUL(d.me, v[p]);
+    }
+}
+
+/* System_Cuspy_Laplace_Nopassing::minimise, detail.h:1694-1753 (see k_nopass_update). */
+extern "C" int fqsb_minimise_nopassing(fqsb_system* h, double tol, uint64_t niter_tol, uint64_t max_iter,
+                                       int max_iter_is_error, uint64_t* ret)
+{
+    if (!h || !ret) {
+        return FQSB_ERR_INVALID;
+    }
+    if (!(tol < 1.0)) {
+        return set_err(h, FQSB_ERR_INVALID, "assertion failed (tol < 1.0)");
+    }
+    if (h->d.pot != POT_CUSPY || h->d.inter != INTER_LAPLACE1D || h->d.N < 2) {
+        return set_err(h, FQSB_ERR_INVALID,
+                       "the no-passing minimiser needs the Cuspy potential on a Line1d ring, N >= 2");
+    }
+    for (int i = 0; i < 5; ++i) {
+        if (!h->fs[i]) {
+            CU(h, cudaMalloc(&h->fs[i], sizeof(double) * (size_t)h->d.N));
+        }
+    }
+    NopassArgs A;
+    A.f_pot = h->fs[0];
+    A.f_int = h->fs[1];
+    A.f_frame = h->fs[2];
+    A.f = h->fs[4];
+    A.den = 2 * h->d.k + h->d.k_frame + h->d.mu;
+    A.ppt = h->lg.ppt;
+    RunResult r; /* (the force arrays, kernel arguments of the graph, live as long as the handle) */
+    int rc = run(h, (int64_t)max_iter, RF_RESID | RF_NOINC, tol, (int64_t)niter_tol, 0.0, 0, 0, nullptr, &r, nullptr,
+                 &A);
+    h->qs_first = h->inc;
+    h->qs_last = h->inc;
+    if (rc) {
+        return rc;
+    }
+    if (r.done == RUN_CONVERGED) {
+        h->stored = false; /* after the quench every force is again a function of the state */
+        rc = quench_impl(h);
+        if (rc) {
+            return rc;
+        }
+        *ret = 0;
+        return sync(h);
+    }
+    /* not converged: the forces are those of the last sweep, f without damping (detail.h:1746) */
+    k_damping_only<<<blocks_for(h->d.N, 256), 256, 0, h->stream>>>(h->d, cur_v(h), h->fs[3]);
+    CU(h, cudaGetLastError());
+    h->stored = true;
+    *ret = max_iter + 1;
+    if (max_iter_is_error) {
+        int rs = sync(h);
+        if (rs) {
+            return rs;
+        }
+        return set_err(h, FQSB_ERR_NO_CONVERGENCE, "No convergence found");
+    }
+    return sync(h);
 }
 
 extern "C" int fqsb_max_uniform_displacement(fqsb_system* h, int direction, double* ret)
@@ -1601,6 +1697,10 @@ extern "C" int fqsb_set_parameters(fqsb_system* h, double mu, double k_interacti
     /* the cached well constants of SemiSmooth depend on mu */
     k_rewell<<<blocks_for(h->d.N, 256), 256, 0, h->stream>>>(h->d);
     CU(h, cudaGetLastError());
+    if (h->graph_np) {
+        cudaGraphExecDestroy(h->graph_np);
+        h->graph_np = nullptr;
+    }
     if (h->graph) {
         cudaGraphExecDestroy(h->graph); /* the parameters are kernel arguments of the run graph */
         h->graph = nullptr;

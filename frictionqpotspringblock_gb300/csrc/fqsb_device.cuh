@@ -59,7 +59,8 @@ constexpr int64_t MAX_WALK = int64_t(1) << 26;
 enum : int { RF_RESID = 1, RF_ACT = 2, RF_FLOW = 4, RF_EVENT = 8, RF_TRUNCATE = 16,
              RF_SCHEDULE = 32, /* u_frame of step i is sched[i] (set before the step, as set_u_frame) */
              RF_RECORD = 64,   /* record each step's output u, v, a and well into rec_* [step][N] */
-             RF_FFSUM = 128 }; /* record each step's sum of f_frame (pairwise order) into rec_ffsum[step] */
+             RF_FFSUM = 128,   /* record each step's sum of f_frame (pairwise order) into rec_ffsum[step] */
+             RF_NOINC = 256 }; /* the loop's iterations are not time steps: inc does not advance */
 
 /* Control block of a stepping run; lives in device memory, written by the host before a run and
  * by the last CTA of every step. */

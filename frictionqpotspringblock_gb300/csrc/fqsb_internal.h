@@ -49,6 +49,16 @@ cudaError_t launch_small_run(const DevSys& s, const SmallGeom& g, cudaStream_t s
 /* Whether a cluster of g.ctas CTAs of this kernel can be co-scheduled (sizes above 8 are opt-in). */
 bool small_cluster_fits(const DevSys& s, const SmallGeom& g);
 
+/* Arguments of the no-passing minimiser's kernels (the force arrays are the handle's stored forces). */
+struct NopassArgs {
+    double *f_pot, *f_int, *f_frame, *f;
+    double den; /* (2 k + k_frame) + mu */
+    int ppt;    /* particles per thread (the step's launch shape, for the canonical residual tree) */
+};
+static const int NOPASS_MAX_REALIGN = 1 << 20; /* bound on one particle's well updates in one sweep */
+cudaError_t build_nopass_graph(const DevSys& s, const LineGeom& g, const NopassArgs& A, cudaGraphExec_t* exec);
+cudaError_t launch_nopass_iteration(const DevSys& s, const LineGeom& g, const NopassArgs& A, cudaStream_t st);
+
 /* One loop iteration launched kernel by kernel by the host (s.in_graph must be 0). */
 cudaError_t launch_iteration(const DevSys& s, const LineGeom& g, cudaStream_t st);
 

@@ -132,7 +132,9 @@ __device__ __forceinline__ void finalize_ctl(CTL* c, double* ring, double uf, do
         c->u_frame = uf;
     }
     c->step += 1;
-    c->inc += 1;
+    if (!(flags & RF_NOINC)) {
+        c->inc += 1;
+    }
     c->cur ^= 1;
     if (flags & RF_FLOW) {
         c->u_frame = uf;
@@ -749,6 +751,107 @@ __global__ void __launch_bounds__(128) k_regen(DevSys s)
     }
 }
 
+/* ------------------------------------------------------------- no-passing minimiser */
+
+/*
+ * minimise of System_Cuspy_Laplace_Nopassing (detail.h:1694-1753, class Line1d.h:173-238): one Jacobi
+ * sweep per loop iteration, in the same run graph form as the dynamics (WHILE node, stop test on the
+ * device).  k_nopass_update: from the previous sweep's positions (buffer cur, the reference's v_n
+ * snapshot) each particle takes
+ *     u = ((k (u[p-1] + u[p+1]) + k_frame u_frame) + mu umin) / ((2 k + k_frame) + mu),
+ * umin the centre of its current well; the chunk is aligned at u (moving the window when needed) and,
+ * while the local chunk index changes, u is recomputed with the new well.  Writes u (buffer cur ^ 1),
+ * f_frame and f_potential.  k_nopass_force: f_interactions of the new positions,
+ * f = (f_potential + f_interactions) + f_frame, the residual subtrees; the last CTA runs the StopList
+ * test (finalize_step with RF_NOINC: no time passes).
+ */
+__global__ void __launch_bounds__(256) k_nopass_update(DevSys s, NopassArgs A)
+{
+    __shared__ StepShared sh;
+    if (!step_prologue(s, sh, true)) {
+        return;
+    }
+    const int cur = sh.cur;
+    const double uf = sh.uf;
+    const int64_t N = s.N;
+    const double* u0 = s.u[cur];
+    const int64_t p0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * A.ppt;
+    for (int j = 0; j < A.ppt; ++j) {
+        const int64_t p = p0 + j;
+        if (p >= N) {
+            break;
+        }
+        const double uneigh = p == 0       ? FQ_ADD(u0[N - 1], u0[1])
+                              : p == N - 1 ? FQ_ADD(u0[N - 2], u0[0])
+                                           : FQ_ADD(u0[p - 1], u0[p + 1]);
+        const double* y = s.data + p * s.W;
+        int64_t i = s.cidx[p];
+        double umin = 0.0, u = 0.0;
+        for (int it = 0;; ++it) {
+            if (it >= NOPASS_MAX_REALIGN) {
+                atomicOr(&s.ctl->walk_flag, 1); /* reported as an error by the finalisation */
+                break;
+            }
+            umin = FQ_MUL(0.5, FQ_ADD(y[i], y[i + 1]));
+            u = FQ_DIV(FQ_ADD(FQ_ADD(FQ_MUL(s.k, uneigh), FQ_MUL(s.k_frame, uf)), FQ_MUL(s.mu, umin)), A.den);
+            dev_align(s, p, u);
+            const int64_t jj = s.cidx[p];
+            if (jj == i) {
+                break;
+            }
+            i = jj;
+        }
+        s.u[cur ^ 1][p] = u;
+        s.v[cur ^ 1][p] = s.v[cur][p];
+        s.a[cur ^ 1][p] = s.a[cur][p];
+        A.f_frame[p] = FQ_MUL(s.k_frame, FQ_SUB(uf, u));
+        A.f_pot[p] = FQ_MUL(s.mu, FQ_SUB(umin, u));
+    }
+}
+
+__global__ void __launch_bounds__(256) k_nopass_force(DevSys s, NopassArgs A)
+{
+    __shared__ StepShared sh;
+    if (!step_prologue(s, sh, true)) {
+        return;
+    }
+    const int cur = sh.cur;
+    const int64_t N = s.N;
+    const double* u1 = s.u[cur ^ 1];
+    const int64_t p0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * A.ppt;
+    double rf = 0.0, rff = 0.0;
+    for (int j = 0; j < A.ppt; ++j) {
+        const int64_t p = p0 + j;
+        if (p >= N) {
+            break;
+        }
+        const double u = u1[p];
+        const double uL = u1[p == 0 ? N - 1 : p - 1], uR = u1[p == N - 1 ? 0 : p + 1];
+        const double fi = scale(FQ_ADD(FQ_SUB(uL, scale_pow2(u, 1, 2.0)), uR), s.s_k);
+        const double ff = A.f_frame[p];
+        const double f = FQ_ADD(FQ_ADD(A.f_pot[p], fi), ff);
+        A.f_int[p] = fi;
+        A.f[p] = f;
+        const double f2 = FQ_MUL(f, f), ff2 = FQ_MUL(ff, ff);
+        if (j == 0) {
+            rf = f2;
+            rff = ff2;
+        }
+        else {
+            rf = FQ_ADD(rf, f2);
+            rff = FQ_ADD(rff, ff2);
+        }
+    }
+    step_epilogue(s, sh, EPI_LINE, rf, rff);
+}
+
+cudaError_t launch_nopass_iteration(const DevSys& s, const LineGeom& g, const NopassArgs& A, cudaStream_t st)
+{
+    k_nopass_update<<<(unsigned)g.grid, (unsigned)g.threads, 0, st>>>(s, A);
+    k_nopass_force<<<(unsigned)g.grid, (unsigned)g.threads, 0, st>>>(s, A);
+    return cudaGetLastError();
+}
+
 /* ------------------------------------------------------------- small systems: one cluster */
 
 /*
@@ -1254,6 +1357,35 @@ cudaError_t build_run_graph(DevSys& s, const LineGeom& g0, cudaGraphExec_t* exec
         GR(add_kernel(&nred, body, &nif, 1, (void*)k_reduce_grid, dim3((unsigned)grid_reduce_ctas(s.N)), dim3(256),
                       argsr));
     }
+    e = cudaGraphInstantiate(exec, g, 0);
+    cudaGraphDestroy(g);
+    return e;
+}
+
+/* The no-passing minimiser's graph: WHILE(h_while) { k_nopass_update ; k_nopass_force }. */
+cudaError_t build_nopass_graph(const DevSys& s0, const LineGeom& g0, const NopassArgs& A, cudaGraphExec_t* exec)
+{
+    DevSys s = s0;
+    cudaGraph_t g;
+    cudaError_t e = cudaGraphCreate(&g, 0);
+    if (e != cudaSuccess) {
+        return e;
+    }
+    cudaGraphConditionalHandle hw;
+    GR(cudaGraphConditionalHandleCreate(&hw, g, 1, cudaGraphCondAssignDefault));
+    cudaGraphNode_t wnode;
+    cudaGraph_t body;
+    GR(add_conditional(&wnode, g, nullptr, 0, hw, cudaGraphCondTypeWhile, &body));
+    s.h_while = hw;
+    s.h_if = 0;
+    s.in_graph = 1;
+    NopassArgs a = A;
+    void* args[] = {(void*)&s, (void*)&a};
+    cudaGraphNode_t nup, nforce;
+    GR(add_kernel(&nup, body, nullptr, 0, (void*)k_nopass_update, dim3((unsigned)g0.grid), dim3((unsigned)g0.threads),
+                  args));
+    GR(add_kernel(&nforce, body, &nup, 1, (void*)k_nopass_force, dim3((unsigned)g0.grid), dim3((unsigned)g0.threads),
+                  args));
     e = cudaGraphInstantiate(exec, g, 0);
     cudaGraphDestroy(g);
     return e;

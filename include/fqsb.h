@@ -111,6 +111,13 @@ int fqsb_time_steps_until_event(fqsb_system* h, double tol, uint64_t niter_tol, 
                                 uint64_t* ret);                    /* timeStepsUntilEvent main.cpp:215-222, detail.h:1595 */
 int fqsb_minimise(fqsb_system* h, double tol, uint64_t niter_tol, uint64_t max_iter, int time_activity,
                   int max_iter_is_error, uint64_t* ret);           /* minimise         main.cpp:161-170, detail.h:1676 */
+/* minimise of Line1d.System_Cuspy_Laplace_Nopassing: the overdamped no-passing fixed point (Jacobi sweeps),
+ * main.cpp:532-568 (class), detail.h:1694-1753 (the Overdamped branch of minimise).  Cuspy + Laplace1d,
+ * N >= 2; inc does not advance; on convergence v = a = 0 (quench), otherwise the forces of the last
+ * sweep are kept (f = (f_potential + f_interactions) + f_frame).  ret: 0 on convergence, else
+ * max_iter + 1 (FQSB_ERR_NO_CONVERGENCE when max_iter_is_error). */
+int fqsb_minimise_nopassing(fqsb_system* h, double tol, uint64_t niter_tol, uint64_t max_iter, int max_iter_is_error,
+                            uint64_t* ret);
 int fqsb_minimise_truncate(fqsb_system* h, const int64_t* i_n, uint64_t A_truncate, uint64_t S_truncate, double tol,
                            uint64_t niter_tol, uint64_t max_iter, int time_activity, int max_iter_is_error,
                            uint64_t* ret);                         /* minimise_truncate main.cpp:172-184, detail.h:1833 */

@@ -1056,6 +1056,83 @@ int oq_minimise_truncate(oq_system* s, const int64_t* i_n, uint64_t A_truncate, 
     return minimise_impl(s, i_n, A_truncate, S_truncate, tol, niter_tol, max_iter, 1, max_iter_is_error, 1, ret);
 }
 
+/*
+ * minimise of System_Cuspy_Laplace_Nopassing, the Overdamped branch of detail.h:1694-1753 (class
+ * Line1d.h:173-238): a Jacobi fixed point over the particles.  From the snapshot v_n = u of the
+ * previous sweep, each particle takes the position that balances its neighbours' springs, the frame
+ * spring and the parabola of its current well,
+ *     u = ((k * (v_n[p-1] + v_n[p+1]) + k_frame * u_frame) + mu * umin) / ((2 * k + k_frame) + mu),
+ * with umin the well's centre 0.5 * (y_i + y_{i+1}); the chunk is aligned at u and, while the local
+ * chunk index changes, the position is recomputed with the new well.  Then f_frame, f_potential
+ * (per particle), f_interactions (after the sweep) and f = (f_potential + f_interactions) + f_frame,
+ * and the StopList residual test; quench on convergence.  Time (inc) does not advance.
+ */
+int oq_minimise_nopassing(oq_system* s, double tol, uint64_t niter_tol, uint64_t max_iter, int max_iter_is_error,
+                          uint64_t* ret)
+{
+    if (s->pot != OQ_CUSPY || s->inter != OQ_LAPLACE1D || s->N < 2) {
+        return fail(s, OQ_ERR_INVALID, "the no-passing minimiser needs the Cuspy potential on a Line1d ring, N >= 2");
+    }
+    double tol2 = tol * tol;
+    stoplist res;
+    sl_init(&res, niter_tol);
+    const int64_t N = s->N, n = s->n;
+    const double k = s->k;
+    const double den = 2 * k + s->k_frame + s->mu;
+    s->qs_first = s->inc_n;
+    s->qs_last = s->inc_n;
+    uint64_t step;
+    int rc = OQ_OK;
+    for (step = 1; step < max_iter + 1; ++step) {
+        memcpy(s->v_n, s->u, sizeof(double) * (size_t)N);
+        for (int64_t p = 0; p < N; ++p) {
+            double uneigh;
+            if (p == 0) {
+                uneigh = s->v_n[N - 1] + s->v_n[1];
+            }
+            else if (p == N - 1) {
+                uneigh = s->v_n[N - 2] + s->v_n[0];
+            }
+            else {
+                uneigh = s->v_n[p - 1] + s->v_n[p + 1];
+            }
+            int64_t i = s->cidx[p];
+            const double* y = s->data + p * n;
+            double umin, u;
+            for (;;) {
+                umin = 0.5 * (y[i] + y[i + 1]);
+                u = (k * uneigh + s->k_frame * s->u_frame + s->mu * umin) / den;
+                align_p(s, p, u);
+                int64_t j = s->cidx[p];
+                if (j == i) {
+                    break;
+                }
+                i = j;
+            }
+            s->u[p] = u;
+            s->f_frame[p] = s->k_frame * (s->u_frame - u);
+            s->f_pot[p] = s->mu * (umin - u);
+        }
+        compute_force_interactions(s);
+        for (int64_t p = 0; p < N; ++p) {
+            s->f[p] = s->f_pot[p] + s->f_int[p] + s->f_frame[p];
+        }
+        sl_insert(&res, residual(s));
+        if ((sl_descending(&res) && sl_all_less(&res, tol)) || sl_all_less(&res, tol2)) {
+            oq_quench(s);
+            *ret = 0;
+            goto out;
+        }
+    }
+    *ret = step;
+    if (max_iter_is_error) {
+        rc = fail(s, OQ_ERR_NO_CONVERGENCE, "No convergence found");
+    }
+out:
+    free(res.r);
+    return rc;
+}
+
 /* maxUniformDisplacement detail.h:1901-1905; Cuspy :176-187; SemiSmooth :282-334; Smooth :414-422 */
 int oq_max_uniform_displacement(oq_system* s, int direction, double* ret)
 {

@@ -104,6 +104,9 @@ int oq_time_step(oq_system* s);
 int oq_time_steps(oq_system* s, uint64_t n);
 int oq_flow_steps(oq_system* s, uint64_t n, double v_frame);
 int oq_time_steps_until_event(oq_system* s, double tol, uint64_t niter_tol, uint64_t max_iter, uint64_t* ret);
+/* System_Cuspy_Laplace_Nopassing::minimise (detail.h:1694-1753) */
+int oq_minimise_nopassing(oq_system* s, double tol, uint64_t niter_tol, uint64_t max_iter, int max_iter_is_error,
+                          uint64_t* ret);
 int oq_minimise(oq_system* s, double tol, uint64_t niter_tol, uint64_t max_iter, int time_activity,
                 int max_iter_is_error, uint64_t* ret);
 int oq_minimise_truncate(oq_system* s, const int64_t* i_n, uint64_t A_truncate, uint64_t S_truncate,

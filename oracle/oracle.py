@@ -107,6 +107,7 @@ def lib():
         L.oq_flow_steps.argtypes = [P, u64, d]
         L.oq_time_steps_until_event.argtypes = [P, d, u64, u64, ctypes.POINTER(u64)]
         L.oq_minimise.argtypes = [P, d, u64, u64, i32, i32, ctypes.POINTER(u64)]
+        L.oq_minimise_nopassing.argtypes = [P, d, u64, u64, i32, ctypes.POINTER(u64)]
         L.oq_minimise_truncate.argtypes = [P, P, u64, u64, d, u64, u64, i32, i32, ctypes.POINTER(u64)]
         L.oq_max_uniform_displacement.argtypes = [P, i32, pd]
         L.oq_event_driven_step.argtypes = [P, d, i32, i32, pd]
@@ -326,6 +327,12 @@ class System:
                                       int(max_iter_is_error), ctypes.byref(r)))
         return r.value
 
+    def minimise_nopassing(self, tol=1e-5, niter_tol=10, max_iter=int(1e9), max_iter_is_error=True):
+        r = ctypes.c_uint64()
+        self._check(lib().oq_minimise_nopassing(self._h, tol, niter_tol, int(max_iter), int(max_iter_is_error),
+                                                ctypes.byref(r)))
+        return r.value
+
     def minimise_truncate(self, i_n, A_truncate=0, S_truncate=0, tol=1e-5, niter_tol=10, max_iter=int(1e9),
                           time_activity=True, max_iter_is_error=True):
         idx = np.ascontiguousarray(i_n, dtype=np.int64).ravel()
@@ -360,6 +367,15 @@ class System:
 def line1d(potential="Cuspy", **kw):
     pot = {"Cuspy": CUSPY, "SemiSmooth": SEMISMOOTH, "Smooth": SMOOTH}[potential]
     return System(pot, LAPLACE1D, **kw)
+
+
+def line1d_nopassing(mu, k_interactions, k_frame, shape, seed, distribution, parameters, offset=-100.0,
+                     nchunk=5000, eta=0.0, dt=0.0, **kw):
+    """System_Cuspy_Laplace_Nopassing (Line1d.h:173-238): Cuspy + Laplace1d with m = 1; minimise it with
+    `minimise_nopassing` (the reference's class has no dynamics)."""
+    return System(CUSPY, LAPLACE1D, m=1.0, eta=eta, mu=mu, k_interactions=k_interactions, k_frame=k_frame, dt=dt,
+                  shape=shape, seed=seed, distribution=distribution, parameters=parameters, offset=offset,
+                  nchunk=nchunk, **kw)
 
 
 def line2d(**kw):

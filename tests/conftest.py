@@ -15,6 +15,12 @@ def pytest_configure(config):
 
 
 def pytest_collection_modifyitems(config, items):
+    # a GPU test that runs away (e.g. a minimise that cannot converge) ends after 5 minutes instead of
+    # holding the GPU; needs pytest-timeout (present here and on the GPU hosts), skipped if absent
+    if config.pluginmanager.hasplugin("timeout"):
+        for item in items:
+            if "gpu" in item.keywords and item.get_closest_marker("timeout") is None:
+                item.add_marker(pytest.mark.timeout(300))
     if os.environ.get("FQSB_SLOW") == "1":
         return
     skip = pytest.mark.skip(reason="slow; set FQSB_SLOW=1")

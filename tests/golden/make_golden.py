@@ -20,6 +20,8 @@ FILES = {
     "Line2d_Cuspy_Laplace": (1000, "x_frame"),
     "Line1d_SemiSmooth_Laplace": (1000, "x_frame"),
     "Particles_Cuspy": (2000, "u_frame"),
+    "Line1d_Cuspy_Laplace_Nopassing": (1000, "x_frame"),
+    "Line1d_Cuspy_Quartic": (1000, "x_frame"),
 }
 
 
