@@ -63,6 +63,35 @@ class System_Smooth_Laplace(System):
                          offset=offset, nchunk=nchunk, **kwargs)
 
 
+class System_Cuspy_Quartic(System):
+    """Cuspy potential + Quartic1d interactions (main.cpp:768-810, Line1d.h:428-481, detail.h:757-805)."""
+
+    _potential = C.CUSPY
+    _interactions = C.QUARTIC1D
+    _rank = 1
+    _name = "Line1d.System_Cuspy_Quartic"
+
+    def __init__(self, m, eta, mu, a1, a2, k_frame, dt, shape, seed, distribution, parameters, offset=-100.0,
+                 nchunk=5000, **kwargs):
+        super().__init__(m, eta, mu, 0.0, k_frame, dt, shape, seed, distribution, parameters, offset=offset,
+                         nchunk=nchunk, interaction_parameters=(a1, a2), **kwargs)
+
+
+class System_Cuspy_QuarticGradient(System):
+    """Cuspy potential + QuarticGradient1d interactions (main.cpp:813-855, Line1d.h:562-615,
+    detail.h:616-653)."""
+
+    _potential = C.CUSPY
+    _interactions = C.QUARTICGRADIENT1D
+    _rank = 1
+    _name = "Line1d.System_Cuspy_QuarticGradient"
+
+    def __init__(self, m, eta, mu, k2, k4, k_frame, dt, shape, seed, distribution, parameters, offset=-100.0,
+                 nchunk=5000, **kwargs):
+        super().__init__(m, eta, mu, 0.0, k_frame, dt, shape, seed, distribution, parameters, offset=offset,
+                         nchunk=nchunk, interaction_parameters=(k2, k4), **kwargs)
+
+
 class _Hidden:
     """A member of the base class that this class does not have (raises AttributeError, hasattr is False)."""
 

@@ -25,7 +25,7 @@ ERR_UNSUPPORTED = 8
 ERR_NO_DEVICE = 9
 
 CUSPY, SEMISMOOTH, SMOOTH = 0, 1, 2
-INTERACTIONS_NONE, LAPLACE1D, LAPLACE2D = 0, 1, 2
+INTERACTIONS_NONE, LAPLACE1D, LAPLACE2D, QUARTIC1D, QUARTICGRADIENT1D, QUARTICGRADIENT2D = 0, 1, 2, 3, 4, 5
 DISTRIBUTIONS = {
     "random": 0,
     "delta": 1,
@@ -63,6 +63,7 @@ class Config(ctypes.Structure):
         ("nchunk", ctypes.c_int64),
         ("stream", ctypes.c_void_p),
         ("device", ctypes.c_int),
+        ("interaction_parameters", ctypes.c_double * 2),
     ]
 
 

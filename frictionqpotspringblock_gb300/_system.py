@@ -100,7 +100,8 @@ class System:
     _name = "System"
 
     def __init__(self, m, eta, mu, k_interactions, k_frame, dt, shape, seed, distribution, parameters,
-                 offset=-100.0, nchunk=5000, kappa=0.0, offset_per_particle=None, stream=None, device=0):
+                 offset=-100.0, nchunk=5000, kappa=0.0, offset_per_particle=None, stream=None, device=0,
+                 interaction_parameters=(0.0, 0.0)):
         shape = [int(i) for i in np.atleast_1d(shape)]
         if len(shape) != self._rank:
             raise ValueError(f"shape must have {self._rank} entries")
@@ -116,6 +117,8 @@ class System:
         cfg.rows, cfg.cols = rows, cols
         cfg.m, cfg.eta, cfg.mu, cfg.kappa = float(m), float(eta), float(mu), float(kappa)
         cfg.k_interactions, cfg.k_frame, cfg.dt = float(k_interactions), float(k_frame), float(dt)
+        cfg.interaction_parameters[0] = float(interaction_parameters[0])
+        cfg.interaction_parameters[1] = float(interaction_parameters[1])
         cfg.seed = int(seed)
         cfg.distribution = C.DISTRIBUTIONS[distribution]
         cfg.n_parameters = len(parameters)

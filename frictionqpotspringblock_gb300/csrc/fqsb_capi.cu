@@ -150,18 +150,7 @@ __device__ __forceinline__ void pi_force(const DevSys& d, const double* u, int64
         case POT_SEMISMOOTH: fp = pot_force<POT_SEMISMOOTH>(d, w, up); break;
         default: fp = pot_force<POT_SMOOTH>(d, w, up); break;
     }
-    fi = 0.0;
-    if (d.inter == INTER_LAPLACE1D) {
-        int64_t N = d.N;
-        double uL = u[p == 0 ? N - 1 : p - 1], uR = u[p == N - 1 ? 0 : p + 1];
-        fi = FQ_MUL(FQ_ADD(FQ_SUB(uL, FQ_MUL(2.0, up)), uR), d.k);
-    }
-    else if (d.inter == INTER_LAPLACE2D) {
-        int64_t R = d.rows, C = d.cols, i = p / C, j = p % C;
-        double uU = u[((i + R - 1) % R) * C + j], uD = u[((i + 1) % R) * C + j];
-        double uL = u[i * C + (j + C - 1) % C], uR = u[i * C + (j + 1) % C];
-        fi = FQ_MUL(FQ_SUB(FQ_ADD(FQ_ADD(FQ_ADD(uU, uD), uL), uR), FQ_MUL(4.0, up)), d.k);
-    }
+    fi = inter_force_at(d, u, p);
 }
 
 /* all force components of particle p from the state (u, v, u_frame) */
@@ -793,11 +782,14 @@ extern "C" int fqsb_create(const fqsb_config* cfg, fqsb_system** out)
     if (cfg->rows < 1 || cfg->cols < 1 || cfg->nchunk < 34 || cfg->n_parameters < 0 || cfg->n_parameters > 4) {
         return set_err(nullptr, FQSB_ERR_INVALID, "invalid shape, nchunk (>= 34) or parameters");
     }
-    if (cfg->potential < 0 || cfg->potential > 2 || cfg->interactions < 0 || cfg->interactions > 2) {
+    if (cfg->potential < 0 || cfg->potential > 2 || cfg->interactions < 0 || cfg->interactions > 5) {
         return set_err(nullptr, FQSB_ERR_INVALID, "invalid potential or interactions");
     }
-    if (cfg->interactions == FQSB_LAPLACE1D && cfg->rows != 1) {
-        return set_err(nullptr, FQSB_ERR_INVALID, "Laplace1d needs rows == 1");
+    if (cfg->interactions >= FQSB_QUARTIC1D && cfg->potential != FQSB_CUSPY) {
+        return set_err(nullptr, FQSB_ERR_UNSUPPORTED, "the Quartic interactions are implemented with the Cuspy potential");
+    }
+    if (inter_ring(cfg->interactions) && cfg->rows != 1) {
+        return set_err(nullptr, FQSB_ERR_INVALID, "Line1d interactions need rows == 1");
     }
     int dist = cfg->distribution;
     if (!(dist == FQSB_DIST_RANDOM || dist == FQSB_DIST_DELTA || dist == FQSB_DIST_EXPONENTIAL ||
@@ -865,6 +857,14 @@ extern "C" int fqsb_create(const fqsb_config* cfg, fqsb_system** out)
     d.mu = cfg->mu;
     d.kappa = cfg->kappa;
     d.k = cfg->k_interactions;
+    d.ia = cfg->interaction_parameters[0];
+    d.ib = cfg->interaction_parameters[1];
+    d.k4_4 = 0.25 * d.ib;            /* QuarticGradient1d::m_k4_4, detail.h:633 */
+    {
+        const double mk4_3 = d.ib / 3.0; /* QuarticGradient2d::force, detail.h:685-686 */
+        d.qg_c2 = d.ia + mk4_3;
+        d.qg_k23 = 2.0 * mk4_3;
+    }
     d.k_frame = cfg->k_frame;
     d.me = -cfg->eta;
     d.m = cfg->m;
@@ -881,7 +881,7 @@ extern "C" int fqsb_create(const fqsb_config* cfg, fqsb_system** out)
     d.buffer = 2;
     d.margin = 30;
     d.min_margin = 6;
-    h->is2d = cfg->interactions == FQSB_LAPLACE2D;
+    h->is2d = inter_grid(cfg->interactions);
     d.s_mu = classify_scale(d.mu);
     d.s_k = classify_scale(d.k);
     d.s_kf = classify_scale(d.k_frame);
@@ -896,7 +896,7 @@ extern "C" int fqsb_create(const fqsb_config* cfg, fqsb_system** out)
         if (h->sg.ok && h->sg.ctas > 8 && !small_cluster_fits(d, h->sg)) {
             h->sg = small_geometry(N, 8); /* the GPU cannot co-schedule a cluster of 16 */
         }
-        h->small_ok = h->sg.ok && cfg->interactions != FQSB_LAPLACE2D && !(ns && ns[0] == '1');
+        h->small_ok = h->sg.ok && !inter_grid(cfg->interactions) && !(ns && ns[0] == '1');
     }
     int64_t nsteps_cta = step_ctas(d, h->lg);
     int64_t npart = h->is2d ? std::max(grid_reduce_ctas(N), nsteps_cta) : h->lg.grid;
@@ -1738,8 +1738,9 @@ extern "C" int fqsb_adjoint_forward(fqsb_system* h, const double* schedule, int6
     if (!h || !schedule || !loss || T < 1 || K < 1 || last < 1 || last > T) {
         return FQSB_ERR_INVALID;
     }
-    if (h->is2d) {
-        return set_err(h, FQSB_ERR_UNSUPPORTED, "the adjoint is implemented for Line1d and Particles systems");
+    if (h->is2d || h->d.inter == INTER_QUARTIC1D || h->d.inter == INTER_QUARTICGRAD1D) {
+        return set_err(h, FQSB_ERR_UNSUPPORTED,
+                       "the adjoint is implemented for Line1d (Laplace1d) and Particles systems");
     }
     int64_t N = h->d.N;
     int64_t nseg = (T + K - 1) / K;

@@ -35,7 +35,24 @@ namespace fqsb {
 constexpr uint64_t PCG_MULT = 0x5851f42d4c957f2dULL;
 
 enum : int { POT_CUSPY = 0, POT_SEMISMOOTH = 1, POT_SMOOTH = 2 };
-enum : int { INTER_NONE = 0, INTER_LAPLACE1D = 1, INTER_LAPLACE2D = 2 };
+enum : int {
+    INTER_NONE = 0,
+    INTER_LAPLACE1D = 1,
+    INTER_LAPLACE2D = 2,
+    INTER_QUARTIC1D = 3,     /* Quartic1d, detail.h:757-805 */
+    INTER_QUARTICGRAD1D = 4, /* QuarticGradient1d, detail.h:616-653 */
+    INTER_QUARTICGRAD2D = 5  /* QuarticGradient2d, detail.h:658-751 */
+};
+
+/* nearest neighbours on a periodic ring / on a periodic rows x cols grid */
+__host__ __device__ constexpr bool inter_ring(int inter)
+{
+    return inter == INTER_LAPLACE1D || inter == INTER_QUARTIC1D || inter == INTER_QUARTICGRAD1D;
+}
+__host__ __device__ constexpr bool inter_grid(int inter)
+{
+    return inter == INTER_LAPLACE2D || inter == INTER_QUARTICGRAD2D;
+}
 enum : int {
     DIST_RANDOM = 0,
     DIST_DELTA = 1,
@@ -119,6 +136,9 @@ struct DevSys {
     int64_t N, rows, cols;
     int pot, inter;
     double dt, hdt, hdt2, mu, kappa, k, k_frame, me, inv_m, m;
+    /* Quartic1d: ia = a1, ib = a2; QuarticGradient: ia = k2, ib = k4, k4_4 = 0.25 k4 (1d),
+     * qg_c2 = k2 + k4 / 3 and qg_k23 = 2 (k4 / 3) (2d), each rounded as the reference forms them */
+    double ia, ib, k4_4, qg_c2, qg_k23;
     Scale s_mu, s_k, s_kf, s_im; /* mu, k_interactions, k_frame, 1/m */
     /* chunk */
     int64_t W, n0;
@@ -658,6 +678,78 @@ __device__ __forceinline__ double pot_force(const DevSys& s, const double4_32a& 
         double arg = FQ_DIV(FQ_MUL(pi, FQ_SUB(up, w.z)), w.w);
         return FQ_MUL(FQ_DIV(FQ_MUL(-s.mu, w.w), pi), fq_sin(arg));
     }
+}
+
+/* ------------------------------------------------ interactions */
+
+/*
+ * f_interactions of a particle on a ring from its own and its two neighbours' positions.
+ * Laplace1d detail.h:474-487 ((uL - 2u) + uR, then times k); Quartic1d :781-803
+ * (a1 ((uL - 2u) + uR) + a2 ((dup dup) dup + (dun dun) dun), dup = uR - u, dun = uL - u);
+ * QuarticGradient1d :636-650 (((uL - 2u) + uR) (k2 + (k4/4 du) du), du = uR - uL).
+ * SOFT selects the integer-pipe forms of the Laplace1d operations (sites 7, 8).
+ */
+template <int INTER, unsigned SOFT = 0u>
+__device__ __forceinline__ double ring_force(const DevSys& s, double uL, double u, double uR)
+{
+    if (INTER == INTER_LAPLACE1D) {
+        return scale(S_ADD(8, S_SUB(7, uL, scale_pow2(u, 1, 2.0)), uR), s.s_k);
+    }
+    const double lap = FQ_ADD(FQ_SUB(uL, scale_pow2(u, 1, 2.0)), uR);
+    if (INTER == INTER_QUARTIC1D) {
+        const double dup = FQ_SUB(uR, u), dun = FQ_SUB(uL, u);
+        return FQ_ADD(FQ_MUL(s.ia, lap),
+                      FQ_MUL(s.ib, FQ_ADD(FQ_MUL(FQ_MUL(dup, dup), dup), FQ_MUL(FQ_MUL(dun, dun), dun))));
+    }
+    const double du = FQ_SUB(uR, uL);
+    return FQ_MUL(lap, FQ_ADD(s.ia, FQ_MUL(FQ_MUL(s.k4_4, du), du)));
+}
+
+/*
+ * QuarticGradient2d (detail.h:677-750) of cell (i, j) from its 3 x 3 neighbourhood: uip = u(i+1, j),
+ * uim = u(i-1, j), ujp = u(i, j+1), ujm = u(i, j-1), upp = u(i+1, j+1), upm = u(i+1, j-1),
+ * ump = u(i-1, j+1), umm = u(i-1, j-1), in the reference's order of operations.
+ */
+__device__ __forceinline__ double qg2d_force(const DevSys& s, double u, double uip, double uim, double ujp, double ujm,
+                                             double upp, double upm, double ump, double umm)
+{
+    const double u2 = scale_pow2(u, 1, 2.0);
+    const double l = FQ_SUB(FQ_ADD(FQ_ADD(FQ_ADD(uip, uim), ujp), ujm), scale_pow2(u, 2, 4.0));
+    const double dudx = FQ_MUL(0.5, FQ_SUB(uip, uim));
+    const double dudy = FQ_MUL(0.5, FQ_SUB(ujp, ujm));
+    const double d2udxdy = FQ_MUL(0.25, FQ_ADD(FQ_SUB(FQ_SUB(upp, upm), ump), umm));
+    const double d2udx2 = FQ_ADD(FQ_SUB(uip, u2), uim);
+    const double d2udy2 = FQ_ADD(FQ_SUB(ujp, u2), ujm);
+    const double t = FQ_ADD(FQ_ADD(FQ_MUL(FQ_MUL(dudx, dudx), d2udx2), FQ_MUL(FQ_MUL(dudy, dudy), d2udy2)),
+                            FQ_MUL(FQ_MUL(FQ_MUL(2.0, dudx), dudy), d2udxdy));
+    return FQ_ADD(FQ_MUL(l, s.qg_c2), FQ_MUL(s.qg_k23, t));
+}
+
+/* f_interactions of particle p from the positions u (any interaction type; no shared memory). */
+__device__ __forceinline__ double inter_force_at(const DevSys& s, const double* u, int64_t p)
+{
+    if (inter_ring(s.inter)) {
+        const int64_t N = s.N;
+        const double uL = u[p == 0 ? N - 1 : p - 1], uR = u[p == N - 1 ? 0 : p + 1];
+        switch (s.inter) {
+            case INTER_LAPLACE1D: return ring_force<INTER_LAPLACE1D>(s, uL, u[p], uR);
+            case INTER_QUARTIC1D: return ring_force<INTER_QUARTIC1D>(s, uL, u[p], uR);
+            default: return ring_force<INTER_QUARTICGRAD1D>(s, uL, u[p], uR);
+        }
+    }
+    if (inter_grid(s.inter)) {
+        const int64_t R = s.rows, C = s.cols, i = p / C, j = p % C;
+        const int64_t im = (i + R - 1) % R, ip = (i + 1) % R, jm = (j + C - 1) % C, jp = (j + 1) % C;
+        if (s.inter == INTER_LAPLACE2D) {
+            /* Laplace2d detail.h:545-583: (((u(i-1,j) + u(i+1,j)) + u(i,j-1)) + u(i,j+1)) - 4 u, then times k */
+            return scale(FQ_SUB(FQ_ADD(FQ_ADD(FQ_ADD(u[im * C + j], u[ip * C + j]), u[i * C + jm]), u[i * C + jp]),
+                                scale_pow2(u[p], 2, 4.0)),
+                         s.s_k);
+        }
+        return qg2d_force(s, u[p], u[ip * C + j], u[im * C + j], u[i * C + jp], u[i * C + jm], u[ip * C + jp],
+                          u[ip * C + jm], u[im * C + jp], u[im * C + jm]);
+    }
+    return 0.0;
 }
 
 /* ------------------------------------------------ canonical reductions */

@@ -502,7 +502,7 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_line(DevSys s
             un[j] = S_ADD(3, S_ADD(2, u0[p0 + j], S_MUL(0, s.dt, vr[j])), S_MUL(1, s.hdt2, ar[j]));
         }
     }
-    if (INTER == INTER_LAPLACE1D) {
+    if (inter_ring(INTER)) {
 #pragma unroll
         for (int j = 0; j < PPT; ++j) {
             sh_un[threadIdx.x * PPT + j] = un[j];
@@ -527,11 +527,11 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_line(DevSys s
         double ff;
         double sfp = frame_pot<POT, SOFT>(s, w, up, uf, ff);
         double fi = 0.0;
-        if (INTER == INTER_LAPLACE1D) {
+        if (inter_ring(INTER)) {
             int li = threadIdx.x * PPT + j;
             double uL = li > 0 ? sh_un[li - 1] : u_next(s, u0, v0, a0, p == 0 ? N - 1 : p - 1);
             double uR = (li + 1 < T * PPT && p + 1 < N) ? sh_un[li + 1] : u_next(s, u0, v0, a0, p + 1 == N ? 0 : p + 1);
-            fi = scale(S_ADD(8, S_SUB(7, uL, scale_pow2(up, 1, 2.0)), uR), s.s_k);
+            fi = ring_force<INTER, SOFT>(s, uL, up, uR);
         }
         double sfi = S_ADD(9, sfp, fi);
         double f;
@@ -604,7 +604,7 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_line(DevSys s
  * written per particle (sq2) and summed in the flat-index pairwise order by k_reduce_grid, which
  * also finalises the step.
  */
-template <int POT, unsigned SOFT = STEP_SOFT>
+template <int POT, int INTER = INTER_LAPLACE2D, unsigned SOFT = STEP_SOFT>
 __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_grid(DevSys s, int redo)
 {
     __shared__ StepShared sh;
@@ -658,11 +658,26 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_grid(DevSys s
         }
         double ff;
         double sfp = frame_pot<POT, SOFT>(s, w, up, uf, ff);
-        double uU = ty > 0 ? sh_un[ty - 1][tx] : u_next(s, u0, v0, a0, ((i + R - 1) % R) * C + jc);
-        double uD = (ty < 7 && i + 1 < R) ? sh_un[ty + 1][tx] : u_next(s, u0, v0, a0, ((i + 1) % R) * C + jc);
-        double uL = tx > 0 ? sh_un[ty][tx - 1] : u_next(s, u0, v0, a0, i * C + (jc + C - 1) % C);
-        double uR = (tx < 31 && jc + 1 < C) ? sh_un[ty][tx + 1] : u_next(s, u0, v0, a0, i * C + (jc + 1) % C);
-        double fi = scale(FQ_SUB(FQ_ADD(FQ_ADD(FQ_ADD(uU, uD), uL), uR), scale_pow2(up, 2, 4.0)), s.s_k);
+        double fi;
+        if (INTER == INTER_LAPLACE2D) {
+            double uU = ty > 0 ? sh_un[ty - 1][tx] : u_next(s, u0, v0, a0, ((i + R - 1) % R) * C + jc);
+            double uD = (ty < 7 && i + 1 < R) ? sh_un[ty + 1][tx] : u_next(s, u0, v0, a0, ((i + 1) % R) * C + jc);
+            double uL = tx > 0 ? sh_un[ty][tx - 1] : u_next(s, u0, v0, a0, i * C + (jc + C - 1) % C);
+            double uR = (tx < 31 && jc + 1 < C) ? sh_un[ty][tx + 1] : u_next(s, u0, v0, a0, i * C + (jc + 1) % C);
+            fi = scale(FQ_SUB(FQ_ADD(FQ_ADD(FQ_ADD(uU, uD), uL), uR), scale_pow2(up, 2, 4.0)), s.s_k);
+        }
+        else {
+            /* 3 x 3 neighbourhood: the tile's new positions, or recomputed from the old state outside it */
+            auto nb = [&](int di, int dj) -> double {
+                const int yy = ty + di, xx = tx + dj;
+                const int64_t ii = i + di, jj = jc + dj;
+                if (yy >= 0 && yy < 8 && xx >= 0 && xx < 32 && ii >= 0 && ii < R && jj >= 0 && jj < C) {
+                    return sh_un[yy][xx];
+                }
+                return u_next(s, u0, v0, a0, ((ii + R) % R) * C + (jj + C) % C);
+            };
+            fi = qg2d_force(s, up, nb(1, 0), nb(-1, 0), nb(0, 1), nb(0, -1), nb(1, 1), nb(1, -1), nb(-1, 1), nb(-1, -1));
+        }
         double sfi = S_ADD(9, sfp, fi);
         double vv, aa, f;
         verlet_velocity<SOFT>(s, sfi, vr, ar, vv, aa, f);
@@ -996,11 +1011,11 @@ __global__ void __launch_bounds__(256) k_run_small(DevSys s)
             double ff;
             double sfp = frame_pot<POT, SOFT>(s, ww, up, uf, ff);
             double fi = 0.0;
-            if (INTER == INTER_LAPLACE1D) {
+            if (inter_ring(INTER)) {
                 int li = tid * PPT + j;
                 double uL = li > 0 ? sh_un[buf][li - 1] : left[buf][il];
                 double uR = (li + 1 < tile && p + 1 < N) ? sh_un[buf][li + 1] : right[buf][ir];
-                fi = scale(S_ADD(8, S_SUB(7, uL, scale_pow2(up, 1, 2.0)), uR), s.s_k);
+                fi = ring_force<INTER, SOFT>(s, uL, up, uR);
             }
             double sfi = S_ADD(9, sfp, fi);
             double vn, an, f;
@@ -1115,6 +1130,13 @@ static const void* small_kernel_t(int ppt)
 
 static const void* small_kernel(const DevSys& s, const SmallGeom& g)
 {
+    /* the Quartic interactions exist with the Cuspy potential only (Line1d.h:428, :562) */
+    if (s.inter == INTER_QUARTIC1D) {
+        return small_kernel_t<POT_CUSPY, INTER_QUARTIC1D>(g.ppt);
+    }
+    if (s.inter == INTER_QUARTICGRAD1D) {
+        return small_kernel_t<POT_CUSPY, INTER_QUARTICGRAD1D>(g.ppt);
+    }
     if (s.inter == INTER_LAPLACE1D) {
         return s.pot == POT_CUSPY ? small_kernel_t<POT_CUSPY, INTER_LAPLACE1D>(g.ppt)
                : s.pot == POT_SEMISMOOTH ? small_kernel_t<POT_SEMISMOOTH, INTER_LAPLACE1D>(g.ppt)
@@ -1200,7 +1222,7 @@ int64_t grid_reduce_ctas(int64_t N)
 
 int64_t step_ctas(const DevSys& s, const LineGeom& g)
 {
-    if (s.inter == INTER_LAPLACE2D) {
+    if (inter_grid(s.inter)) {
         return ((s.cols + 31) / 32) * ((s.rows + 7) / 8);
     }
     return g.grid;
@@ -1216,6 +1238,15 @@ static void* line_kernel_t(int ppt)
 
 static void* step_kernel(const DevSys& s, const LineGeom& g)
 {
+    if (s.inter == INTER_QUARTICGRAD2D) {
+        return (void*)k_step_grid<POT_CUSPY, INTER_QUARTICGRAD2D>;
+    }
+    if (s.inter == INTER_QUARTIC1D) {
+        return line_kernel_t<POT_CUSPY, INTER_QUARTIC1D>(g.ppt);
+    }
+    if (s.inter == INTER_QUARTICGRAD1D) {
+        return line_kernel_t<POT_CUSPY, INTER_QUARTICGRAD1D>(g.ppt);
+    }
     if (s.inter == INTER_LAPLACE2D) {
         switch (s.pot) {
             case POT_CUSPY: return (void*)k_step_grid<POT_CUSPY>;
@@ -1272,7 +1303,7 @@ static cudaError_t add_conditional(cudaGraphNode_t* node, cudaGraph_t graph, con
  */
 cudaError_t launch_iteration(const DevSys& s, const LineGeom& g0, cudaStream_t st)
 {
-    bool is2d = s.inter == INTER_LAPLACE2D;
+    bool is2d = inter_grid(s.inter);
     dim3 grid, block;
     if (is2d) {
         grid = dim3((unsigned)((s.cols + 31) / 32), (unsigned)((s.rows + 7) / 8));
@@ -1330,7 +1361,7 @@ cudaError_t build_run_graph(DevSys& s, const LineGeom& g0, cudaGraphExec_t* exec
     s.h_if = hi;
     s.in_graph = 1;
 
-    bool is2d = s.inter == INTER_LAPLACE2D;
+    bool is2d = inter_grid(s.inter);
     dim3 grid, block;
     if (is2d) {
         grid = dim3((unsigned)((s.cols + 31) / 32), (unsigned)((s.rows + 7) / 8));

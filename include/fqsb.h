@@ -41,7 +41,14 @@ typedef enum {
 /* potential (detail.h:113 Cuspy, :212 SemiSmooth, :356 Smooth) */
 enum { FQSB_CUSPY = 0, FQSB_SEMISMOOTH = 1, FQSB_SMOOTH = 2 };
 /* interactions (none = Particles.h:93-311; detail.h:446 Laplace1d; :524 Laplace2d) */
-enum { FQSB_INTERACTIONS_NONE = 0, FQSB_LAPLACE1D = 1, FQSB_LAPLACE2D = 2 };
+enum {
+    FQSB_INTERACTIONS_NONE = 0,
+    FQSB_LAPLACE1D = 1,          /* detail.h:446-488 */
+    FQSB_LAPLACE2D = 2,          /* detail.h:524-584 */
+    FQSB_QUARTIC1D = 3,          /* detail.h:757-805, Line1d.System_Cuspy_Quartic (main.cpp:768-810) */
+    FQSB_QUARTICGRADIENT1D = 4,  /* detail.h:616-653, Line1d.System_Cuspy_QuarticGradient (main.cpp:813-855) */
+    FQSB_QUARTICGRADIENT2D = 5   /* detail.h:658-751, Line2d.System_Cuspy_QuarticGradient (main.cpp:963-1005) */
+};
 /* distributions, prrng names (detail.h:31-66) */
 enum {
     FQSB_DIST_RANDOM = 0,
@@ -83,7 +90,7 @@ enum {
  */
 typedef struct {
     int potential;           /* FQSB_CUSPY / FQSB_SEMISMOOTH / FQSB_SMOOTH */
-    int interactions;        /* FQSB_INTERACTIONS_NONE / FQSB_LAPLACE1D / FQSB_LAPLACE2D */
+    int interactions;        /* FQSB_INTERACTIONS_NONE / FQSB_LAPLACE1D / FQSB_LAPLACE2D / FQSB_QUARTIC* */
     int64_t rows, cols;      /* 1d: rows = 1, cols = N */
     double m, eta, mu, kappa, k_interactions, k_frame, dt;
     uint64_t seed;           /* particle p uses pcg32(initstate = seed + p, initseq = 0) */
@@ -95,6 +102,7 @@ typedef struct {
     int64_t nchunk;          /* yield positions held per particle (>= 34) */
     void* stream;            /* cudaStream_t to run on, or NULL for a private stream */
     int device;              /* CUDA device ordinal */
+    double interaction_parameters[2]; /* Quartic1d: a1, a2; QuarticGradient1d / 2d: k2, k4 (Laplace: unused) */
 } fqsb_config;
 
 /* Lifecycle. */

@@ -41,6 +41,7 @@ struct oq_system {
     int pot, inter;
     int64_t rows, cols, N, n;
     double m, inv_m, eta, mu, kappa, k, k_frame, dt;
+    double ia, ib; /* Quartic1d: a1, a2; QuarticGradient1d / 2d: k2, k4 */
     int dist, npar;
     double par[4];
     double offset;
@@ -452,6 +453,47 @@ static void compute_force_interactions(oq_system* s)
             f[p] *= s->k;
         }
     }
+    else if (s->inter == OQ_QUARTIC1D) {
+        /* Quartic1d::force, detail.h:781-803 */
+        for (int64_t p = 0; p < N; ++p) {
+            int64_t l = p == 0 ? N - 1 : p - 1;
+            int64_t r = p == N - 1 ? 0 : p + 1;
+            double dup = u[r] - u[p];
+            double dun = u[l] - u[p];
+            f[p] = s->ia * (u[l] - 2 * u[p] + u[r]) + s->ib * (dup * dup * dup + dun * dun * dun);
+        }
+    }
+    else if (s->inter == OQ_QUARTICGRAD1D) {
+        /* QuarticGradient1d::force, detail.h:636-650 (m_k4_4 = 0.25 * k4, :633) */
+        double k4_4 = 0.25 * s->ib;
+        for (int64_t p = 0; p < N; ++p) {
+            int64_t l = p == 0 ? N - 1 : p - 1;
+            int64_t r = p == N - 1 ? 0 : p + 1;
+            double du = u[r] - u[l];
+            f[p] = (u[l] - 2 * u[p] + u[r]) * (s->ia + k4_4 * du * du);
+        }
+    }
+    else if (s->inter == OQ_QUARTICGRAD2D) {
+        /* QuarticGradient2d::force, detail.h:677-750 (periodic neighbours) */
+        int64_t R = s->rows, C = s->cols;
+        double mk4_3 = s->ib / 3.0;
+        double mk4_23 = 2.0 * mk4_3;
+        for (int64_t i = 0; i < R; ++i) {
+            int64_t im = (i + R - 1) % R, ip = (i + 1) % R;
+            for (int64_t j = 0; j < C; ++j) {
+                int64_t jm = (j + C - 1) % C, jp = (j + 1) % C;
+                double c = u[i * C + j];
+                double l = u[ip * C + j] + u[im * C + j] + u[i * C + jp] + u[i * C + jm] - 4 * c;
+                double dudx = 0.5 * (u[ip * C + j] - u[im * C + j]);
+                double dudy = 0.5 * (u[i * C + jp] - u[i * C + jm]);
+                double d2udxdy = 0.25 * (u[ip * C + jp] - u[ip * C + jm] - u[im * C + jp] + u[im * C + jm]);
+                double d2udx2 = u[ip * C + j] - 2 * c + u[im * C + j];
+                double d2udy2 = u[i * C + jp] - 2 * c + u[i * C + jm];
+                f[i * C + j] = l * (s->ia + mk4_3) +
+                               mk4_23 * (dudx * dudx * d2udx2 + dudy * dudy * d2udy2 + 2.0 * dudx * dudy * d2udxdy);
+            }
+        }
+    }
     else if (s->inter == OQ_LAPLACE2D) {
         int64_t R = s->rows, C = s->cols;
         for (int64_t i = 0; i < R; ++i) {
@@ -506,6 +548,14 @@ static void updated_v(oq_system* s)
 {
     compute_force_damping(s);
     compute_force(s);
+}
+
+/* parameters of the Quartic interactions (System_Cuspy_Quartic / _QuarticGradient constructors) */
+int oq_set_interaction_parameters(oq_system* s, double a, double b)
+{
+    s->ia = a;
+    s->ib = b;
+    return oq_refresh(s);
 }
 
 /* ------------------------------------------------------- lifecycle */

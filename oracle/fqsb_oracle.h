@@ -38,6 +38,9 @@ typedef struct oq_system oq_system;
 #define OQ_NONE 0
 #define OQ_LAPLACE1D 1
 #define OQ_LAPLACE2D 2
+#define OQ_QUARTIC1D 3
+#define OQ_QUARTICGRAD1D 4
+#define OQ_QUARTICGRAD2D 5
 /* distributions (prrng names) */
 #define OQ_DIST_RANDOM 0
 #define OQ_DIST_DELTA 1
@@ -107,6 +110,7 @@ int oq_time_steps_until_event(oq_system* s, double tol, uint64_t niter_tol, uint
 /* System_Cuspy_Laplace_Nopassing::minimise (detail.h:1694-1753) */
 int oq_minimise_nopassing(oq_system* s, double tol, uint64_t niter_tol, uint64_t max_iter, int max_iter_is_error,
                           uint64_t* ret);
+int oq_set_interaction_parameters(oq_system* s, double a, double b);
 int oq_minimise(oq_system* s, double tol, uint64_t niter_tol, uint64_t max_iter, int time_activity,
                 int max_iter_is_error, uint64_t* ret);
 int oq_minimise_truncate(oq_system* s, const int64_t* i_n, uint64_t A_truncate, uint64_t S_truncate,

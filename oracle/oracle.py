@@ -24,7 +24,7 @@ LIB = BUILD / "libfqsb_oracle.so"
 SOURCES = [HERE / "fqsb_oracle.c", HERE / "fqsb_oracle.h", HERE.parent / "frictionqpotspringblock_gb300" / "csrc" / "fq_math.h"]
 
 CUSPY, SEMISMOOTH, SMOOTH = 0, 1, 2
-NONE, LAPLACE1D, LAPLACE2D = 0, 1, 2
+NONE, LAPLACE1D, LAPLACE2D, QUARTIC1D, QUARTICGRAD1D, QUARTICGRAD2D = 0, 1, 2, 3, 4, 5
 SUM_SEQUENTIAL, SUM_PAIRWISE = 0, 1
 MATH_LIBM, MATH_PORTABLE = 0, 1
 DISTRIBUTIONS = {
@@ -108,6 +108,7 @@ def lib():
         L.oq_time_steps_until_event.argtypes = [P, d, u64, u64, ctypes.POINTER(u64)]
         L.oq_minimise.argtypes = [P, d, u64, u64, i32, i32, ctypes.POINTER(u64)]
         L.oq_minimise_nopassing.argtypes = [P, d, u64, u64, i32, ctypes.POINTER(u64)]
+        L.oq_set_interaction_parameters.argtypes = [P, d, d]
         L.oq_minimise_truncate.argtypes = [P, P, u64, u64, d, u64, u64, i32, i32, ctypes.POINTER(u64)]
         L.oq_max_uniform_displacement.argtypes = [P, i32, pd]
         L.oq_event_driven_step.argtypes = [P, d, i32, i32, pd]
@@ -221,7 +222,7 @@ class System:
 
     def __init__(self, potential, interactions, shape, m, eta, mu, k_interactions, k_frame, dt, seed,
                  distribution, parameters, offset=-100.0, nchunk=5000, kappa=0.0, offset_per_particle=None,
-                 sum_mode=SUM_PAIRWISE, math_mode=MATH_PORTABLE):
+                 sum_mode=SUM_PAIRWISE, math_mode=MATH_PORTABLE, interaction_parameters=None):
         shape = [int(i) for i in shape]
         rows, cols = (1, shape[0]) if len(shape) == 1 else (shape[0], shape[1])
         self.shape = shape
@@ -238,6 +239,9 @@ class System:
         if not h:
             raise OracleError("invalid oracle configuration")
         self._h = h
+        if interaction_parameters is not None:
+            a, b = (float(x) for x in interaction_parameters)
+            self._check(lib().oq_set_interaction_parameters(h, a, b))
         self.dt, self.mu, self.eta, self.m, self.k_frame = dt, mu, eta, m, k_frame
         self.chunk = _Chunk(self)
 
@@ -376,6 +380,26 @@ def line1d_nopassing(mu, k_interactions, k_frame, shape, seed, distribution, par
     return System(CUSPY, LAPLACE1D, m=1.0, eta=eta, mu=mu, k_interactions=k_interactions, k_frame=k_frame, dt=dt,
                   shape=shape, seed=seed, distribution=distribution, parameters=parameters, offset=offset,
                   nchunk=nchunk, **kw)
+
+
+def line1d_quartic(m, eta, mu, a1, a2, k_frame, dt, shape, seed, distribution, parameters, **kw):
+    """System_Cuspy_Quartic (Line1d.h:428-481)."""
+    return System(CUSPY, QUARTIC1D, shape=shape, m=m, eta=eta, mu=mu, k_interactions=0.0, k_frame=k_frame, dt=dt,
+                  seed=seed, distribution=distribution, parameters=parameters, interaction_parameters=(a1, a2), **kw)
+
+
+def line1d_quartic_gradient(m, eta, mu, k2, k4, k_frame, dt, shape, seed, distribution, parameters, **kw):
+    """Line1d System_Cuspy_QuarticGradient (Line1d.h:562-615)."""
+    return System(CUSPY, QUARTICGRAD1D, shape=shape, m=m, eta=eta, mu=mu, k_interactions=0.0, k_frame=k_frame,
+                  dt=dt, seed=seed, distribution=distribution, parameters=parameters, interaction_parameters=(k2, k4),
+                  **kw)
+
+
+def line2d_quartic_gradient(m, eta, mu, k2, k4, k_frame, dt, shape, seed, distribution, parameters, **kw):
+    """Line2d System_Cuspy_QuarticGradient (Line2d.h:122-167)."""
+    return System(CUSPY, QUARTICGRAD2D, shape=shape, m=m, eta=eta, mu=mu, k_interactions=0.0, k_frame=k_frame,
+                  dt=dt, seed=seed, distribution=distribution, parameters=parameters, interaction_parameters=(k2, k4),
+                  **kw)
 
 
 def line2d(**kw):

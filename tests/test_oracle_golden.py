@@ -1,7 +1,8 @@
 """The oracle against the reference's historic golden trajectories.
 
 The reference's examples/{Line1d_Cuspy_Laplace,Line2d_Cuspy_Laplace,
-Line1d_SemiSmooth_Laplace,Particles_Cuspy,Line1d_Cuspy_Laplace_Nopassing}.py run an event-driven quasistatic
+Line1d_SemiSmooth_Laplace,Particles_Cuspy,Line1d_Cuspy_Laplace_Nopassing,
+Line1d_Cuspy_Quartic}.py run an event-driven quasistatic
 protocol and assert np.allclose on the frame position and the mean frame force,
 and exact equality of the avalanche size S, against stored .h5 files
 (examples/Line1d_Cuspy_Laplace.py:35-67).  The same protocol runs here through
@@ -28,6 +29,9 @@ def make(which, sum_mode, math_mode=O.MATH_LIBM):
         return O.line1d("SemiSmooth", shape=[1000], k_interactions=1.0, k_frame=1.0 / 1000, kappa=1.0, **common)
     if which == "Line2d_Cuspy_Laplace":
         return O.line2d(shape=[50, 50], k_interactions=1.0, k_frame=1.0 / 2500, **common)
+    if which == "Line1d_Cuspy_Quartic":
+        # examples/Line1d_Cuspy_Quartic.py:17-31
+        return O.line1d_quartic(shape=[1000], a1=1.0, a2=1.0, k_frame=1.0 / 1000, **common)
     if which == "Line1d_Cuspy_Laplace_Nopassing":
         # examples/Line1d_Cuspy_Laplace_Nopassing.py:17-26 (m = 1, eta = dt = 0)
         return O.line1d_nopassing(mu=1.0, k_interactions=1.0, k_frame=1.0 / 1000, shape=[1000], seed=0,
@@ -56,6 +60,7 @@ CASES = [
     ("Line2d_Cuspy_Laplace", 60),
     ("Particles_Cuspy", 300),
     ("Line1d_Cuspy_Laplace_Nopassing", 1000),
+    ("Line1d_Cuspy_Quartic", 100),
 ]
 
 
