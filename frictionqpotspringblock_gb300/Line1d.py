@@ -92,6 +92,21 @@ class System_Cuspy_QuarticGradient(System):
                          nchunk=nchunk, interaction_parameters=(k2, k4), **kwargs)
 
 
+class System_Cuspy_LongRange(System):
+    """Cuspy potential + LongRange1d interactions, all pairs decaying as 1 / d^(1 + alpha)
+    (main.cpp:857-897, Line1d.h:617-675, detail.h:812-868)."""
+
+    _potential = C.CUSPY
+    _interactions = C.LONGRANGE1D
+    _rank = 1
+    _name = "Line1d.System_Cuspy_LongRange"
+
+    def __init__(self, m, eta, mu, k_interactions, alpha, k_frame, dt, shape, seed, distribution, parameters,
+                 offset=-100.0, nchunk=5000, **kwargs):
+        super().__init__(m, eta, mu, k_interactions, k_frame, dt, shape, seed, distribution, parameters,
+                         offset=offset, nchunk=nchunk, interaction_parameters=(alpha, 0.0), **kwargs)
+
+
 class _Hidden:
     """A member of the base class that this class does not have (raises AttributeError, hasattr is False)."""
 

@@ -25,7 +25,7 @@ ERR_UNSUPPORTED = 8
 ERR_NO_DEVICE = 9
 
 CUSPY, SEMISMOOTH, SMOOTH = 0, 1, 2
-INTERACTIONS_NONE, LAPLACE1D, LAPLACE2D, QUARTIC1D, QUARTICGRADIENT1D, QUARTICGRADIENT2D = 0, 1, 2, 3, 4, 5
+INTERACTIONS_NONE, LAPLACE1D, LAPLACE2D, QUARTIC1D, QUARTICGRADIENT1D, QUARTICGRADIENT2D, LONGRANGE1D = range(7)
 DISTRIBUTIONS = {
     "random": 0,
     "delta": 1,

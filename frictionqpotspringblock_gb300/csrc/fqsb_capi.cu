@@ -745,7 +745,7 @@ static void free_all(fqsb_system* h)
     DevSys& d = h->d;
     void* ptrs[] = {d.data, d.start, d.cidx, d.gidx, d.wc, d.acc_end, d.anc_kind, d.anc_k, d.anc_state, d.anc_val,
                     d.u[0], d.u[1], d.v[0], d.v[1], d.a[0], d.a[1], d.ctl, d.ring, d.partials, d.i_n, d.sq2,
-                    d.cta_pending, d.regen_list,
+                    d.cta_pending, d.regen_list, (void*)d.lr_pref,
                     (void*)d.offp, h->scratch, h->red_partials, h->red_out, h->mkey, h->mflag, h->fs[0], h->fs[1],
                     h->fs[2], h->fs[3], h->fs[4], h->adj_sched, h->adj_ckpt, h->adj_ffsum, h->adj_final};
     for (void* p : ptrs) {
@@ -782,13 +782,14 @@ extern "C" int fqsb_create(const fqsb_config* cfg, fqsb_system** out)
     if (cfg->rows < 1 || cfg->cols < 1 || cfg->nchunk < 34 || cfg->n_parameters < 0 || cfg->n_parameters > 4) {
         return set_err(nullptr, FQSB_ERR_INVALID, "invalid shape, nchunk (>= 34) or parameters");
     }
-    if (cfg->potential < 0 || cfg->potential > 2 || cfg->interactions < 0 || cfg->interactions > 5) {
+    if (cfg->potential < 0 || cfg->potential > 2 || cfg->interactions < 0 || cfg->interactions > 6) {
         return set_err(nullptr, FQSB_ERR_INVALID, "invalid potential or interactions");
     }
     if (cfg->interactions >= FQSB_QUARTIC1D && cfg->potential != FQSB_CUSPY) {
-        return set_err(nullptr, FQSB_ERR_UNSUPPORTED, "the Quartic interactions are implemented with the Cuspy potential");
+        return set_err(nullptr, FQSB_ERR_UNSUPPORTED,
+                       "the Quartic and LongRange interactions are implemented with the Cuspy potential");
     }
-    if (inter_ring(cfg->interactions) && cfg->rows != 1) {
+    if ((inter_ring(cfg->interactions) || cfg->interactions == FQSB_LONGRANGE1D) && cfg->rows != 1) {
         return set_err(nullptr, FQSB_ERR_INVALID, "Line1d interactions need rows == 1");
     }
     int dist = cfg->distribution;
@@ -896,7 +897,8 @@ extern "C" int fqsb_create(const fqsb_config* cfg, fqsb_system** out)
         if (h->sg.ok && h->sg.ctas > 8 && !small_cluster_fits(d, h->sg)) {
             h->sg = small_geometry(N, 8); /* the GPU cannot co-schedule a cluster of 16 */
         }
-        h->small_ok = h->sg.ok && !inter_grid(cfg->interactions) && !(ns && ns[0] == '1');
+        h->small_ok = h->sg.ok && !inter_grid(cfg->interactions) && cfg->interactions != FQSB_LONGRANGE1D &&
+                      !(ns && ns[0] == '1');
     }
     int64_t nsteps_cta = step_ctas(d, h->lg);
     int64_t npart = h->is2d ? std::max(grid_reduce_ctas(N), nsteps_cta) : h->lg.grid;
@@ -932,6 +934,21 @@ extern "C" int fqsb_create(const fqsb_config* cfg, fqsb_system** out)
     }
     ALLOC(d.ctl, sizeof(Ctl));
     ALLOC(d.partials, sizeof(double2) * (size_t)npart);
+    if (d.inter == INTER_LONGRANGE1D) {
+        /* LongRange1d constructor, detail.h:828-841: k / std::pow(d, alpha + 1) on the host */
+        std::vector<double> pref((size_t)N);
+        for (int64_t dd = 0; dd < N; ++dd) {
+            pref[(size_t)dd] = dd == 0 ? 0.0 : d.k / std::pow((double)dd, d.ia + 1.0);
+        }
+        double* dp = nullptr;
+        ALLOC(dp, sizeof(double) * (size_t)N);
+        d.lr_pref = dp;
+        d.lr_m = (N - N % 2) / 2;
+        if (cudaMemcpy(dp, pref.data(), sizeof(double) * (size_t)N, cudaMemcpyHostToDevice) != cudaSuccess) {
+            free_all(h);
+            return set_err(nullptr, FQSB_ERR_CUDA, "cudaMemcpy failed");
+        }
+    }
     ALLOC(d.i_n, sizeof(int64_t) * (size_t)N);
     ALLOC(d.cta_pending, sizeof(int32_t) * (size_t)nsteps_cta);
     ALLOC(d.regen_list, sizeof(int32_t) * (size_t)N);
@@ -1738,7 +1755,8 @@ extern "C" int fqsb_adjoint_forward(fqsb_system* h, const double* schedule, int6
     if (!h || !schedule || !loss || T < 1 || K < 1 || last < 1 || last > T) {
         return FQSB_ERR_INVALID;
     }
-    if (h->is2d || h->d.inter == INTER_QUARTIC1D || h->d.inter == INTER_QUARTICGRAD1D) {
+    if (h->is2d || h->d.inter == INTER_QUARTIC1D || h->d.inter == INTER_QUARTICGRAD1D ||
+        h->d.inter == INTER_LONGRANGE1D) {
         return set_err(h, FQSB_ERR_UNSUPPORTED,
                        "the adjoint is implemented for Line1d (Laplace1d) and Particles systems");
     }

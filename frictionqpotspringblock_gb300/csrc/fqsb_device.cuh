@@ -41,7 +41,8 @@ enum : int {
     INTER_LAPLACE2D = 2,
     INTER_QUARTIC1D = 3,     /* Quartic1d, detail.h:757-805 */
     INTER_QUARTICGRAD1D = 4, /* QuarticGradient1d, detail.h:616-653 */
-    INTER_QUARTICGRAD2D = 5  /* QuarticGradient2d, detail.h:658-751 */
+    INTER_QUARTICGRAD2D = 5, /* QuarticGradient2d, detail.h:658-751 */
+    INTER_LONGRANGE1D = 6    /* LongRange1d, detail.h:812-868 (all pairs on the ring) */
 };
 
 /* nearest neighbours on a periodic ring / on a periodic rows x cols grid */
@@ -139,6 +140,8 @@ struct DevSys {
     /* Quartic1d: ia = a1, ib = a2; QuarticGradient: ia = k2, ib = k4, k4_4 = 0.25 k4 (1d),
      * qg_c2 = k2 + k4 / 3 and qg_k23 = 2 (k4 / 3) (2d), each rounded as the reference forms them */
     double ia, ib, k4_4, qg_c2, qg_k23;
+    const double* lr_pref; /* LongRange1d: k / d^(alpha + 1) by ring distance d (0 at d = 0), host std::pow */
+    int64_t lr_m;          /* LongRange1d: ring distances above lr_m wrap to N - d */
     Scale s_mu, s_k, s_kf, s_im; /* mu, k_interactions, k_frame, 1/m */
     /* chunk */
     int64_t W, n0;
@@ -736,6 +739,23 @@ __device__ __forceinline__ double inter_force_at(const DevSys& s, const double* 
             case INTER_QUARTIC1D: return ring_force<INTER_QUARTIC1D>(s, uL, u[p], uR);
             default: return ring_force<INTER_QUARTICGRAD1D>(s, uL, u[p], uR);
         }
+    }
+    if (s.inter == INTER_LONGRANGE1D) {
+        /* LongRange1d::force detail.h:844-866: sequential sum over i != p in index order */
+        const int64_t N = s.N;
+        const double up = u[p];
+        double fp = 0.0;
+        for (int64_t i = 0; i < N; ++i) {
+            if (i == p) {
+                continue;
+            }
+            int64_t d = i > p ? i - p : p - i;
+            if (d > s.lr_m) {
+                d = N - d;
+            }
+            fp = FQ_ADD(fp, FQ_MUL(FQ_SUB(u[i], up), s.lr_pref[d]));
+        }
+        return fp;
     }
     if (inter_grid(s.inter)) {
         const int64_t R = s.rows, C = s.cols, i = p / C, j = p % C;

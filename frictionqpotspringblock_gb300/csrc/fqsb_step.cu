@@ -766,6 +766,142 @@ __global__ void __launch_bounds__(128) k_regen(DevSys s)
     }
 }
 
+/* ------------------------------------------------------------- long-range interactions */
+
+/*
+ * Line1d System_Cuspy_LongRange (Line1d.h:617-675): every particle interacts with all others,
+ * f_int(p) = sum over i != p, in index order, of (u'(i) - u'(p)) k / d^(alpha+1), d the ring distance
+ * (LongRange1d::force, detail.h:844-866).  All new positions are needed before any interaction, so
+ * the step is two launches: k_lr_position writes u' for all particles; k_lr_step (same pass-1 / redo
+ * roles and epilogue as k_step_line) reads the new positions through shared-memory tiles, keeps each
+ * particle's sum in the reference's sequential order, and does wells, forces, velocity updates and
+ * the residual.
+ */
+__global__ void __launch_bounds__(256) k_lr_position(DevSys s)
+{
+    __shared__ StepShared sh;
+    if (!step_prologue(s, sh, true)) {
+        return;
+    }
+    const int cur = sh.cur;
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < s.N) {
+        s.u[cur ^ 1][p] = u_next(s, s.u[cur], s.v[cur], s.a[cur], p);
+    }
+}
+
+template <int POT, int PPT>
+__global__ void __launch_bounds__(256) k_lr_step(DevSys s, int redo)
+{
+    constexpr int LR_TILE = 1024;
+    __shared__ StepShared sh;
+    __shared__ double tile[LR_TILE];
+    if (!step_prologue(s, sh, true)) {
+        return;
+    }
+    if (redo) {
+        if (!s.cta_pending[blockIdx.x]) {
+            return;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            s.cta_pending[blockIdx.x] = 0;
+        }
+    }
+    const int cur = sh.cur;
+    const bool act = (sh.flags & (RF_ACT | RF_TRUNCATE | RF_EVENT)) != 0;
+    const bool resid = (sh.flags & RF_RESID) != 0;
+    const double uf = sh.uf;
+    const int64_t N = s.N;
+    const int64_t p0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * PPT;
+    const double* un = s.u[cur ^ 1];
+    double up[PPT], fi[PPT];
+#pragma unroll
+    for (int j = 0; j < PPT; ++j) {
+        up[j] = p0 + j < N ? un[p0 + j] : 0.0;
+        fi[j] = 0.0;
+    }
+    for (int64_t t0 = 0; t0 < N; t0 += LR_TILE) {
+        const int cnt = (int)(N - t0 < LR_TILE ? N - t0 : LR_TILE);
+        __syncthreads();
+        for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
+            tile[k] = un[t0 + k];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < PPT; ++j) {
+            const int64_t p = p0 + j;
+            if (p >= N) {
+                continue;
+            }
+            double acc = fi[j];
+            for (int k = 0; k < cnt; ++k) {
+                const int64_t i = t0 + k;
+                if (i == p) {
+                    continue;
+                }
+                int64_t d = i > p ? i - p : p - i;
+                if (d > s.lr_m) {
+                    d = N - d;
+                }
+                acc = FQ_ADD(acc, FQ_MUL(FQ_SUB(tile[k], up[j]), __ldg(s.lr_pref + d)));
+            }
+            fi[j] = acc;
+        }
+    }
+    double rf = 0.0, rff = 0.0;
+    bool nan = false, pending = false;
+#pragma unroll
+    for (int j = 0; j < PPT; ++j) {
+        const int64_t p = p0 + j;
+        if (p >= N) {
+            continue;
+        }
+        bool regen;
+        double4_32a w = well_of(s, p, up[j], act, sh, regen);
+        pending |= regen;
+        double ff;
+        double sfp = frame_pot<POT>(s, w, up[j], uf, ff);
+        double sfi = FQ_ADD(sfp, fi[j]);
+        double vo, ao, f;
+        verlet_velocity(s, sfi, s.v[cur][p], s.a[cur][p], vo, ao, f);
+        s.v[cur ^ 1][p] = vo;
+        s.a[cur ^ 1][p] = ao;
+        nan |= is_nan_bits(up[j]);
+        if (resid) {
+            double f2 = fq_smul(f, f), ff2 = fq_smul(ff, ff);
+            if (j == 0) {
+                rf = f2;
+                rff = ff2;
+            }
+            else {
+                rf = add_nospec(rf, f2);
+                rff = add_nospec(rff, ff2);
+            }
+        }
+    }
+    if (nan) {
+        sh.nan = 1;
+    }
+    if (pending && !redo) {
+        sh.pending = 1;
+        for (int j = 0; j < PPT; ++j) {
+            const int64_t p = p0 + j;
+            if (p < N) {
+                double4_32a w = s.wc[p];
+                if (!in_well(w.x, w.y, up[j]) && !non_finite(up[j])) {
+                    int k = atomicAdd(&s.ctl->n_regen, 1);
+                    s.regen_list[k] = (int32_t)p;
+                }
+            }
+        }
+    }
+    if (pending && redo) {
+        atomicOr(&s.ctl->walk_flag, 1);
+    }
+    step_epilogue(s, sh, redo ? EPI_REDO : EPI_LINE, rf, rff);
+}
+
 /* ------------------------------------------------------------- no-passing minimiser */
 
 /*
@@ -1238,6 +1374,9 @@ static void* line_kernel_t(int ppt)
 
 static void* step_kernel(const DevSys& s, const LineGeom& g)
 {
+    if (s.inter == INTER_LONGRANGE1D) {
+        return g.ppt == 2 ? (void*)k_lr_step<POT_CUSPY, 2> : (void*)k_lr_step<POT_CUSPY, 1>;
+    }
     if (s.inter == INTER_QUARTICGRAD2D) {
         return (void*)k_step_grid<POT_CUSPY, INTER_QUARTICGRAD2D>;
     }
@@ -1318,7 +1457,13 @@ cudaError_t launch_iteration(const DevSys& s, const LineGeom& g0, cudaStream_t s
     void* args1[] = {(void*)&s, (void*)&pass1};
     void* args2[] = {(void*)&s, (void*)&pass2};
     void* argsr[] = {(void*)&s};
-    cudaError_t e = cudaLaunchKernel(fstep, grid, block, args1, 0, st);
+    cudaError_t e = cudaSuccess;
+    if (s.inter == INTER_LONGRANGE1D) {
+        e = cudaLaunchKernel((void*)k_lr_position, dim3((unsigned)((s.N + 255) / 256)), dim3(256), argsr, 0, st);
+    }
+    if (e == cudaSuccess) {
+        e = cudaLaunchKernel(fstep, grid, block, args1, 0, st);
+    }
     if (e == cudaSuccess) {
         e = cudaLaunchKernel((void*)k_regen, dim3(4 * 152), dim3(128), argsr, 0, st);
     }
@@ -1377,7 +1522,16 @@ cudaError_t build_run_graph(DevSys& s, const LineGeom& g0, cudaGraphExec_t* exec
     void* args2[] = {(void*)&s, (void*)&pass2};
     void* argsr[] = {(void*)&s};
     cudaGraphNode_t nstep, nif;
-    GR(add_kernel(&nstep, body, nullptr, 0, fstep, grid, block, args1));
+    if (s.inter == INTER_LONGRANGE1D) {
+        /* all new positions before the all-pairs interaction */
+        cudaGraphNode_t npos;
+        GR(add_kernel(&npos, body, nullptr, 0, (void*)k_lr_position, dim3((unsigned)((s.N + 255) / 256)), dim3(256),
+                      argsr));
+        GR(add_kernel(&nstep, body, &npos, 1, fstep, grid, block, args1));
+    }
+    else {
+        GR(add_kernel(&nstep, body, nullptr, 0, fstep, grid, block, args1));
+    }
     cudaGraph_t ifbody;
     GR(add_conditional(&nif, body, &nstep, 1, hi, cudaGraphCondTypeIf, &ifbody));
     cudaGraphNode_t nregen, nredo;

@@ -47,7 +47,8 @@ enum {
     FQSB_LAPLACE2D = 2,          /* detail.h:524-584 */
     FQSB_QUARTIC1D = 3,          /* detail.h:757-805, Line1d.System_Cuspy_Quartic (main.cpp:768-810) */
     FQSB_QUARTICGRADIENT1D = 4,  /* detail.h:616-653, Line1d.System_Cuspy_QuarticGradient (main.cpp:813-855) */
-    FQSB_QUARTICGRADIENT2D = 5   /* detail.h:658-751, Line2d.System_Cuspy_QuarticGradient (main.cpp:963-1005) */
+    FQSB_QUARTICGRADIENT2D = 5,  /* detail.h:658-751, Line2d.System_Cuspy_QuarticGradient (main.cpp:963-1005) */
+    FQSB_LONGRANGE1D = 6         /* detail.h:812-868, Line1d.System_Cuspy_LongRange (main.cpp:857-897) */
 };
 /* distributions, prrng names (detail.h:31-66) */
 enum {
@@ -102,7 +103,8 @@ typedef struct {
     int64_t nchunk;          /* yield positions held per particle (>= 34) */
     void* stream;            /* cudaStream_t to run on, or NULL for a private stream */
     int device;              /* CUDA device ordinal */
-    double interaction_parameters[2]; /* Quartic1d: a1, a2; QuarticGradient1d / 2d: k2, k4 (Laplace: unused) */
+    double interaction_parameters[2]; /* Quartic1d: a1, a2; QuarticGradient1d / 2d: k2, k4; LongRange1d: alpha
+                                         (with k_interactions); Laplace: unused */
 } fqsb_config;
 
 /* Lifecycle. */

@@ -41,7 +41,9 @@ struct oq_system {
     int pot, inter;
     int64_t rows, cols, N, n;
     double m, inv_m, eta, mu, kappa, k, k_frame, dt;
-    double ia, ib; /* Quartic1d: a1, a2; QuarticGradient1d / 2d: k2, k4 */
+    double ia, ib; /* Quartic1d: a1, a2; QuarticGradient1d / 2d: k2, k4; LongRange1d: alpha */
+    double* lr_pref; /* LongRange1d: k / d^(alpha + 1) for ring distance d (0 for d = 0) */
+    int64_t lr_m;    /* LongRange1d: the midpoint (N - N % 2) / 2 */
     int dist, npar;
     double par[4];
     double offset;
@@ -453,6 +455,25 @@ static void compute_force_interactions(oq_system* s)
             f[p] *= s->k;
         }
     }
+    else if (s->inter == OQ_LONGRANGE1D) {
+        /* LongRange1d::force, detail.h:844-866: sequential sum over i != p in index order (before
+         * oq_set_interaction_parameters gives alpha the interaction is off) */
+        for (int64_t p = 0; p < N && s->lr_pref; ++p) {
+            double fp = 0.0;
+            double up = u[p];
+            for (int64_t i = 0; i < N; ++i) {
+                if (i == p) {
+                    continue;
+                }
+                int64_t d = i > p ? i - p : p - i;
+                if (d > s->lr_m) {
+                    d = N - d;
+                }
+                fp += (u[i] - up) * s->lr_pref[d];
+            }
+            f[p] = fp;
+        }
+    }
     else if (s->inter == OQ_QUARTIC1D) {
         /* Quartic1d::force, detail.h:781-803 */
         for (int64_t p = 0; p < N; ++p) {
@@ -555,6 +576,16 @@ int oq_set_interaction_parameters(oq_system* s, double a, double b)
 {
     s->ia = a;
     s->ib = b;
+    if (s->inter == OQ_LONGRANGE1D) {
+        /* LongRange1d constructor, detail.h:828-841 (alpha = a, k = k_interactions, std::pow) */
+        int64_t n = s->N;
+        free(s->lr_pref);
+        s->lr_pref = (double*)malloc(sizeof(double) * (size_t)n);
+        s->lr_m = (n - n % 2) / 2;
+        for (int64_t d = 0; d < n; ++d) {
+            s->lr_pref[d] = d == 0 ? 0.0 : s->k / pow((double)d, a + 1.0);
+        }
+    }
     return oq_refresh(s);
 }
 
@@ -657,6 +688,7 @@ void oq_destroy(oq_system* s)
     free(s->f_frame);
     free(s->f_damp);
     free(s->tmp);
+    free(s->lr_pref);
     free(s);
 }
 

@@ -41,6 +41,7 @@ typedef struct oq_system oq_system;
 #define OQ_QUARTIC1D 3
 #define OQ_QUARTICGRAD1D 4
 #define OQ_QUARTICGRAD2D 5
+#define OQ_LONGRANGE1D 6
 /* distributions (prrng names) */
 #define OQ_DIST_RANDOM 0
 #define OQ_DIST_DELTA 1

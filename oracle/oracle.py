@@ -24,7 +24,7 @@ LIB = BUILD / "libfqsb_oracle.so"
 SOURCES = [HERE / "fqsb_oracle.c", HERE / "fqsb_oracle.h", HERE.parent / "frictionqpotspringblock_gb300" / "csrc" / "fq_math.h"]
 
 CUSPY, SEMISMOOTH, SMOOTH = 0, 1, 2
-NONE, LAPLACE1D, LAPLACE2D, QUARTIC1D, QUARTICGRAD1D, QUARTICGRAD2D = 0, 1, 2, 3, 4, 5
+NONE, LAPLACE1D, LAPLACE2D, QUARTIC1D, QUARTICGRAD1D, QUARTICGRAD2D, LONGRANGE1D = 0, 1, 2, 3, 4, 5, 6
 SUM_SEQUENTIAL, SUM_PAIRWISE = 0, 1
 MATH_LIBM, MATH_PORTABLE = 0, 1
 DISTRIBUTIONS = {
@@ -400,6 +400,13 @@ def line2d_quartic_gradient(m, eta, mu, k2, k4, k_frame, dt, shape, seed, distri
     return System(CUSPY, QUARTICGRAD2D, shape=shape, m=m, eta=eta, mu=mu, k_interactions=0.0, k_frame=k_frame,
                   dt=dt, seed=seed, distribution=distribution, parameters=parameters, interaction_parameters=(k2, k4),
                   **kw)
+
+
+def line1d_longrange(m, eta, mu, k_interactions, alpha, k_frame, dt, shape, seed, distribution, parameters, **kw):
+    """System_Cuspy_LongRange (Line1d.h:617-675, LongRange1d detail.h:812-868)."""
+    return System(CUSPY, LONGRANGE1D, shape=shape, m=m, eta=eta, mu=mu, k_interactions=k_interactions,
+                  k_frame=k_frame, dt=dt, seed=seed, distribution=distribution, parameters=parameters,
+                  interaction_parameters=(alpha, 0.0), **kw)
 
 
 def line2d(**kw):

@@ -22,6 +22,7 @@ FILES = {
     "Particles_Cuspy": (2000, "u_frame"),
     "Line1d_Cuspy_Laplace_Nopassing": (1000, "x_frame"),
     "Line1d_Cuspy_Quartic": (1000, "x_frame"),
+    "Line1d_Cuspy_Laplace_LongRange": (200, "x_frame"),
 }
 
 

@@ -2,7 +2,7 @@
 
 The reference's examples/{Line1d_Cuspy_Laplace,Line2d_Cuspy_Laplace,
 Line1d_SemiSmooth_Laplace,Particles_Cuspy,Line1d_Cuspy_Laplace_Nopassing,
-Line1d_Cuspy_Quartic}.py run an event-driven quasistatic
+Line1d_Cuspy_Quartic,Line1d_Cuspy_Laplace_LongRange}.py run an event-driven quasistatic
 protocol and assert np.allclose on the frame position and the mean frame force,
 and exact equality of the avalanche size S, against stored .h5 files
 (examples/Line1d_Cuspy_Laplace.py:35-67).  The same protocol runs here through
@@ -29,6 +29,9 @@ def make(which, sum_mode, math_mode=O.MATH_LIBM):
         return O.line1d("SemiSmooth", shape=[1000], k_interactions=1.0, k_frame=1.0 / 1000, kappa=1.0, **common)
     if which == "Line2d_Cuspy_Laplace":
         return O.line2d(shape=[50, 50], k_interactions=1.0, k_frame=1.0 / 2500, **common)
+    if which == "Line1d_Cuspy_Laplace_LongRange":
+        # examples/Line1d_Cuspy_Laplace_LongRange.py:17-30
+        return O.line1d_longrange(shape=[1000], k_interactions=1.0, alpha=1, k_frame=1.0 / 1000, **common)
     if which == "Line1d_Cuspy_Quartic":
         # examples/Line1d_Cuspy_Quartic.py:17-31
         return O.line1d_quartic(shape=[1000], a1=1.0, a2=1.0, k_frame=1.0 / 1000, **common)
@@ -61,6 +64,7 @@ CASES = [
     ("Particles_Cuspy", 300),
     ("Line1d_Cuspy_Laplace_Nopassing", 1000),
     ("Line1d_Cuspy_Quartic", 100),
+    ("Line1d_Cuspy_Laplace_LongRange", 8),
 ]
 
 
