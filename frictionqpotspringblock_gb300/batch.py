@@ -44,6 +44,25 @@ def log_uniform_sizes(n_instances: int = 4096, lo: int = 256, hi: int = 65536, s
     return np.rint(np.exp(a + u * (b - a))).astype(np.int64)
 
 
+def partition(sizes, world: int):
+    """Split realisations over `world` ranks with no exchange between them: longest-processing-time
+    greedy on the sizes (largest first, each to the rank with the least total so far; ties to the
+    lowest rank).  Returns one sorted index array per rank; every realisation appears exactly once.
+    A rank builds its batch from sizes[idx], seeds[idx] and runs independently; results are placed
+    back by idx (weak scaling: no collective on the data path)."""
+    sizes = np.asarray(sizes, dtype=np.int64)
+    if world < 1:
+        raise ValueError("world must be >= 1")
+    order = np.argsort(-sizes, kind="stable")
+    load = np.zeros(world, dtype=np.int64)
+    owner = np.empty(len(sizes), dtype=np.int64)
+    for j in order:
+        r = int(np.argmin(load))
+        owner[j] = r
+        load[r] += sizes[j]
+    return [np.flatnonzero(owner == r) for r in range(world)]
+
+
 class Line1d_System_Cuspy_Laplace:
     """A batch of independent Line1d System_Cuspy_Laplace realisations.
 
