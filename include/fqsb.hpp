@@ -49,7 +49,8 @@ protected:
 
     void init(int potential, int interactions, int64_t rows, int64_t cols, double m, double eta, double mu,
               double kappa, double k_interactions, double k_frame, double dt, uint64_t seed,
-              const std::string& distribution, const std::vector<double>& parameters, double offset, size_t nchunk)
+              const std::string& distribution, const std::vector<double>& parameters, double offset, size_t nchunk,
+              double ip0 = 0.0, double ip1 = 0.0)
     {
         if (parameters.size() > 4) {
             throw std::runtime_error("at most 4 distribution parameters");
@@ -77,6 +78,8 @@ protected:
         c.nchunk = (int64_t)nchunk;
         c.stream = nullptr;
         c.device = 0;
+        c.interaction_parameters[0] = ip0;
+        c.interaction_parameters[1] = ip1;
         if (fqsb_create(&c, &m_h) != FQSB_OK) {
             throw std::runtime_error(fqsb_last_error(nullptr));
         }
@@ -258,6 +261,68 @@ public:
     }
 };
 
+/* Line1d.h:173-238: Cuspy + Laplace1d minimised with the no-passing rule (m = 1, no dynamics) */
+class System_Cuspy_Laplace_Nopassing : public System {
+public:
+    System_Cuspy_Laplace_Nopassing(double mu, double k_interactions, double k_frame, const std::array<size_t, 1>& shape,
+                                   uint64_t seed, const std::string& distribution,
+                                   const std::vector<double>& parameters, double offset = -100.0,
+                                   size_t nchunk = 5000, double eta = 0.0, double dt = 0.0)
+    {
+        init(FQSB_CUSPY, FQSB_LAPLACE1D, 1, (int64_t)shape[0], 1.0, eta, mu, 0.0, k_interactions, k_frame, dt, seed,
+             distribution, parameters, offset, nchunk);
+    }
+
+    /* detail.h:1694-1753 */
+    size_t minimise(double tol = 1e-5, size_t niter_tol = 10, size_t max_iter = 1e9, bool time_activity = false,
+                    bool max_iter_is_error = true)
+    {
+        if (time_activity) {
+            throw std::runtime_error("assertion failed (!time_activity)");
+        }
+        uint64_t r = 0;
+        check(fqsb_minimise_nopassing(m_h, tol, niter_tol, max_iter, max_iter_is_error, &r));
+        return (size_t)r;
+    }
+};
+
+/* Line1d.h:428-481 */
+class System_Cuspy_Quartic : public System {
+public:
+    System_Cuspy_Quartic(double m, double eta, double mu, double a1, double a2, double k_frame, double dt,
+                         const std::array<size_t, 1>& shape, uint64_t seed, const std::string& distribution,
+                         const std::vector<double>& parameters, double offset = -100.0, size_t nchunk = 5000)
+    {
+        init(FQSB_CUSPY, FQSB_QUARTIC1D, 1, (int64_t)shape[0], m, eta, mu, 0.0, 0.0, k_frame, dt, seed, distribution,
+             parameters, offset, nchunk, a1, a2);
+    }
+};
+
+/* Line1d.h:562-615 */
+class System_Cuspy_QuarticGradient : public System {
+public:
+    System_Cuspy_QuarticGradient(double m, double eta, double mu, double k2, double k4, double k_frame, double dt,
+                                 const std::array<size_t, 1>& shape, uint64_t seed, const std::string& distribution,
+                                 const std::vector<double>& parameters, double offset = -100.0, size_t nchunk = 5000)
+    {
+        init(FQSB_CUSPY, FQSB_QUARTICGRADIENT1D, 1, (int64_t)shape[0], m, eta, mu, 0.0, 0.0, k_frame, dt, seed,
+             distribution, parameters, offset, nchunk, k2, k4);
+    }
+};
+
+/* Line1d.h:617-675 */
+class System_Cuspy_LongRange : public System {
+public:
+    System_Cuspy_LongRange(double m, double eta, double mu, double k_interactions, double alpha, double k_frame,
+                           double dt, const std::array<size_t, 1>& shape, uint64_t seed,
+                           const std::string& distribution, const std::vector<double>& parameters,
+                           double offset = -100.0, size_t nchunk = 5000)
+    {
+        init(FQSB_CUSPY, FQSB_LONGRANGE1D, 1, (int64_t)shape[0], m, eta, mu, 0.0, k_interactions, k_frame, dt, seed,
+             distribution, parameters, offset, nchunk, alpha, 0.0);
+    }
+};
+
 } // namespace Line1d
 
 namespace Line2d {
@@ -271,6 +336,18 @@ public:
     {
         init(FQSB_CUSPY, FQSB_LAPLACE2D, (int64_t)shape[0], (int64_t)shape[1], m, eta, mu, 0.0, k_interactions,
              k_frame, dt, seed, distribution, parameters, offset, nchunk);
+    }
+};
+
+/* Line2d.h:122-167 */
+class System_Cuspy_QuarticGradient : public System {
+public:
+    System_Cuspy_QuarticGradient(double m, double eta, double mu, double k2, double k4, double k_frame, double dt,
+                                 const std::array<size_t, 2>& shape, uint64_t seed, const std::string& distribution,
+                                 const std::vector<double>& parameters, double offset = -100.0, size_t nchunk = 5000)
+    {
+        init(FQSB_CUSPY, FQSB_QUARTICGRADIENT2D, (int64_t)shape[0], (int64_t)shape[1], m, eta, mu, 0.0, 0.0, k_frame,
+             dt, seed, distribution, parameters, offset, nchunk, k2, k4);
     }
 };
 

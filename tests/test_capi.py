@@ -51,3 +51,35 @@ def test_create_without_gpu_fails_cleanly(lib):
     with pytest.raises(FrictionError, match="no CUDA device"):
         Line1d.System_Cuspy_Laplace(m=1, eta=1, mu=1, k_interactions=1, k_frame=0.1, dt=1, shape=[5], seed=0,
                                     distribution="delta", parameters=[1.0], offset=-49.5, nchunk=100)
+
+
+def test_cpp_header_compiles(tmp_path):
+    """include/fqsb.hpp (header-only C++ classes over the C ABI) compiles with every class used."""
+    import shutil
+    import subprocess
+
+    if shutil.which("g++") is None:
+        pytest.skip("needs g++")
+    src = tmp_path / "use_hpp.cpp"
+    src.write_text("""
+#include "fqsb.hpp"
+using namespace FrictionQPotSpringBlock_gb300;
+template <class T> void touch(T* s) { if (s) { s->minimise(); s->u(); } }
+int main()
+{
+    touch<Line1d::System_Cuspy_Laplace>(nullptr);
+    touch<Line1d::System_SemiSmooth_Laplace>(nullptr);
+    touch<Line1d::System_Smooth_Laplace>(nullptr);
+    touch<Line1d::System_Cuspy_Laplace_Nopassing>(nullptr);
+    touch<Line1d::System_Cuspy_Quartic>(nullptr);
+    touch<Line1d::System_Cuspy_QuarticGradient>(nullptr);
+    touch<Line1d::System_Cuspy_LongRange>(nullptr);
+    touch<Line2d::System_Cuspy_Laplace>(nullptr);
+    touch<Line2d::System_Cuspy_QuarticGradient>(nullptr);
+    touch<Particles::System_Cuspy>(nullptr);
+    return 0;
+}
+""")
+    inc = pathlib.Path(__file__).resolve().parent.parent / "include"
+    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", f"-I{inc}", str(src)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
