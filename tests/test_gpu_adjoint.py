@@ -5,7 +5,7 @@ set before every step (detail.h:1539-1570).  The torch reference below restates 
 torch float64 operations (wells held at the forward's, read from the system), so torch autograd
 gives an independent gradient.  Tolerances: 1e-9 relative against torch (same FP64 maths, different
 summation order and sin/cos rounding), 1e-6 relative against central finite differences (h = 1e-6),
-the benchmark spec's bar.
+the gradient-error requirement of the differentiation workload.
 """
 
 import math
