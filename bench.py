@@ -124,7 +124,9 @@ class ClockSampler:
 def bench_batched(fqsb, n_inst=512, n_loop=32):
     """Batched form on the first n_inst realisations of the 4096-realisation size list (log-uniform in
     [256, 65536] from pcg32 seed 3; seed 1000+j; k_frame = 1/N_j; Weibull(2,1)+1e-5; 1000-position
-    chunk), one quasistatic cycle each; against looping the plain path over the first n_loop."""
+    chunk), one quasistatic cycle each, with the tile shape the autotuner picks; against looping the
+    plain path over the first n_loop."""
+    from frictionqpotspringblock_gb300 import autotune as A
     from frictionqpotspringblock_gb300 import batch as B
 
     par = dict(m=1.0, eta=0.1, mu=1.0, k_interactions=1.0, dt=0.1, distribution="weibull",
@@ -132,8 +134,17 @@ def bench_batched(fqsb, n_inst=512, n_loop=32):
     sizes = B.log_uniform_sizes(4096, 256, 65536, seed=3)
     seeds = 1000 + np.arange(4096)
     out = {}
+
+    # tile shape (threads x particles per thread) from the autotuner: timed on a sample of the batch
+    def make(sz, threads, ppt):
+        return B.Line1d_System_Cuspy_Laplace(sz, 1000 + np.arange(len(sz)), 1.0 / sz, nchunk=1000, window=64,
+                                             threads=threads, ppt=ppt, **par)
+
+    t0 = time.perf_counter()
+    threads, ppt = A.choose_tile(sizes[:n_inst], make, use_cache=False)
+    out.update(tile=[int(threads), int(ppt)], autotune_seconds=time.perf_counter() - t0)
     b = B.Line1d_System_Cuspy_Laplace(sizes[:n_inst], seeds[:n_inst], 1.0 / sizes[:n_inst], nchunk=1000, window=64,
-                                      threads=256, ppt=1, **par)
+                                      threads=threads, ppt=ppt, **par)
     t0 = time.perf_counter()
     r = b.quasistatic(1, 1e-5)
     t = time.perf_counter() - t0
@@ -141,7 +152,7 @@ def bench_batched(fqsb, n_inst=512, n_loop=32):
     out.update(realisations=n_inst, particles=int(sizes[:n_inst].sum()), seconds=t, particle_steps=ps, value=ps / t)
     del b
     b = B.Line1d_System_Cuspy_Laplace(sizes[:n_loop], seeds[:n_loop], 1.0 / sizes[:n_loop], nchunk=1000, window=64,
-                                      threads=256, ppt=1, **par)
+                                      threads=threads, ppt=ppt, **par)
     t0 = time.perf_counter()
     r = b.quasistatic(1, 1e-5)
     tb = time.perf_counter() - t0
