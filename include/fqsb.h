@@ -192,7 +192,7 @@ int fqsb_adjoint_backward(fqsb_system* h, double* grad_u0, double* grad_v0, doub
  * k_interactions, dt, distribution, offset, nchunk) on one GPU.  No counterpart in the reference,
  * which runs one System at a time; each realisation follows exactly the plain path's arithmetic.
  * `window` (34 <= window <= nchunk) is the number of yield positions kept per particle; the yield
- * sequence does not depend on it.  threads (32..256) x ppt (1 or 2) is the tile (0: defaults).
+ * sequence does not depend on it.  threads (32..256) x ppt (1 or 2) is the tile (0: defaults, 256 x 2).
  */
 typedef struct {
     int64_t n_instances;
