@@ -43,6 +43,12 @@ struct oq_system {
     double m, inv_m, eta, mu, kappa, k, k_frame, dt;
     double ia, ib; /* Quartic1d: a1, a2; QuarticGradient1d / 2d: k2, k4; LongRange1d: alpha */
     double* lr_pref; /* LongRange1d: k / d^(alpha + 1) for ring distance d (0 for d = 0) */
+    /* RandomNormalForcing (detail.h:881-1000): one pcg32 stream drawn in particle order */
+    int thermal, th_mode;
+    double th_mean, th_std;
+    uint64_t th_state, th_inc;
+    int64_t *th_next, *th_dinc;
+    double* f_th;
     int64_t lr_m;    /* LongRange1d: the midpoint (N - N % 2) / 2 */
     int dist, npar;
     double par[4];
@@ -547,12 +553,89 @@ static void compute_force_damping(oq_system* s)
     }
 }
 
-/* computeForce detail.h:1321-1330 (External = void) */
+/* computeForce detail.h:1321-1330 (with External: + f_thermal) */
 static void compute_force(oq_system* s)
 {
     for (int64_t p = 0; p < s->N; ++p) {
         s->f[p] = s->f_frame[p] + s->f_pot[p] + s->f_int[p] + s->f_damp[p];
     }
+    if (s->thermal) {
+        for (int64_t p = 0; p < s->N; ++p) {
+            s->f[p] = s->f[p] + s->f_th[p];
+        }
+    }
+}
+
+/* inverse error function: a starting value refined by Newton steps on libm's erf (test tooling) */
+static double erfinv_d(double y)
+{
+    if (y <= -1.0) {
+        return -INFINITY;
+    }
+    if (y >= 1.0) {
+        return INFINITY;
+    }
+    double w = -log((1.0 - y) * (1.0 + y)), x;
+    if (w < 5.0) {
+        w -= 2.5;
+        x = 2.81022636e-08;
+        x = 3.43273939e-07 + x * w;
+        x = -3.5233877e-06 + x * w;
+        x = -4.39150654e-06 + x * w;
+        x = 0.00021858087 + x * w;
+        x = -0.00125372503 + x * w;
+        x = -0.00417768164 + x * w;
+        x = 0.246640727 + x * w;
+        x = 1.50140941 + x * w;
+    }
+    else {
+        w = sqrt(w) - 3.0;
+        x = -0.000200214257;
+        x = 0.000100950558 + x * w;
+        x = 0.00134934322 + x * w;
+        x = -0.00367342844 + x * w;
+        x = 0.00573950773 + x * w;
+        x = -0.0076224613 + x * w;
+        x = 0.00943887047 + x * w;
+        x = 1.00167406 + x * w;
+        x = 2.83297682 + x * w;
+    }
+    x *= y;
+    for (int i = 0; i < 4; ++i) {
+        double err = erf(x) - y;
+        x -= err / (1.1283791670955126 * exp(-x * x));
+    }
+    return x;
+}
+
+static double thermal_draw(oq_system* s)
+{
+    uint64_t old = s->th_state;
+    s->th_state = old * PCG_MULT + s->th_inc;
+    uint32_t xs = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+    uint32_t rot = (uint32_t)(old >> 59u);
+    uint32_t u32 = (xs >> rot) | (xs << ((-rot) & 31));
+    double r = (double)u32 * 0x1p-32;
+    double z = erfinv_d(2.0 * r - 1.0);
+    if (s->th_mode == 1) {
+        return s->th_mean + s->th_std * (M_SQRT2 * z);
+    }
+    return s->th_mean + (s->th_std * M_SQRT2) * z;
+}
+
+/* updated_inc detail.h:1369-1375 with RandomNormalForcing::force detail.h:930-942 */
+static void updated_inc(oq_system* s)
+{
+    if (!s->thermal) {
+        return;
+    }
+    for (int64_t p = 0; p < s->N; ++p) {
+        if (s->inc_n >= s->th_next[p]) {
+            s->f_th[p] = thermal_draw(s);
+            s->th_next[p] += s->th_dinc[p];
+        }
+    }
+    compute_force(s);
 }
 
 /* updated_u detail.h:1380-1386 */
@@ -689,6 +772,9 @@ void oq_destroy(oq_system* s)
     free(s->f_damp);
     free(s->tmp);
     free(s->lr_pref);
+    free(s->th_next);
+    free(s->th_dinc);
+    free(s->f_th);
     free(s);
 }
 
@@ -791,6 +877,44 @@ int oq_set_inc(oq_system* s, int64_t inc)
     s->qs_first = inc;
     s->qs_last = inc;
     compute_force(s);
+    updated_inc(s);
+    return OQ_OK;
+}
+
+/*
+ * Attach a RandomNormalForcing (Line1d.h:264-330): mean, stddev, the pcg32 (state, inc) after
+ * seeding, per-particle first increment `next` and interval `dinc`; then updated_inc as initSystem's
+ * refresh does (detail.h:1310-1315).  `mode` selects the normal transform's association (exploratory:
+ * prrng's normal transform is not in the reference tree).
+ */
+int oq_set_thermal(oq_system* s, double mean, double stddev, uint64_t state, uint64_t inc, const int64_t* next,
+                   const int64_t* dinc, int mode)
+{
+    int64_t N = s->N;
+    s->thermal = 1;
+    s->th_mode = mode;
+    s->th_mean = mean;
+    s->th_std = stddev;
+    s->th_state = state;
+    s->th_inc = inc;
+    free(s->th_next);
+    free(s->th_dinc);
+    free(s->f_th);
+    s->th_next = (int64_t*)malloc(sizeof(int64_t) * (size_t)N);
+    s->th_dinc = (int64_t*)malloc(sizeof(int64_t) * (size_t)N);
+    s->f_th = (double*)calloc((size_t)N, sizeof(double));
+    memcpy(s->th_next, next, sizeof(int64_t) * (size_t)N);
+    memcpy(s->th_dinc, dinc, sizeof(int64_t) * (size_t)N);
+    updated_inc(s);
+    return OQ_OK;
+}
+
+int oq_get_thermal(oq_system* s, double* f_thermal)
+{
+    if (!s->thermal) {
+        return fail(s, OQ_ERR_INVALID, "no RandomNormalForcing attached");
+    }
+    memcpy(f_thermal, s->f_th, sizeof(double) * (size_t)s->N);
     return OQ_OK;
 }
 
@@ -884,6 +1008,7 @@ int oq_refresh(oq_system* s)
     updated_u(s);
     updated_v(s);
     compute_force(s);
+    updated_inc(s);
     return OQ_OK;
 }
 
@@ -902,6 +1027,7 @@ int oq_time_step(oq_system* s)
     int64_t N = s->N;
     double dt = s->dt, hdt = 0.5 * dt, hdt2 = 0.5 * dt * dt;
     s->inc_n++;
+    updated_inc(s);
     memcpy(s->v_n, s->v, sizeof(double) * (size_t)N);
     memcpy(s->a_n, s->a, sizeof(double) * (size_t)N);
     for (int64_t p = 0; p < N; ++p) {

@@ -112,6 +112,9 @@ int oq_time_steps_until_event(oq_system* s, double tol, uint64_t niter_tol, uint
 int oq_minimise_nopassing(oq_system* s, double tol, uint64_t niter_tol, uint64_t max_iter, int max_iter_is_error,
                           uint64_t* ret);
 int oq_set_interaction_parameters(oq_system* s, double a, double b);
+int oq_set_thermal(oq_system* s, double mean, double stddev, uint64_t state, uint64_t inc, const int64_t* next,
+                   const int64_t* dinc, int mode);
+int oq_get_thermal(oq_system* s, double* f_thermal);
 int oq_minimise(oq_system* s, double tol, uint64_t niter_tol, uint64_t max_iter, int time_activity,
                 int max_iter_is_error, uint64_t* ret);
 int oq_minimise_truncate(oq_system* s, const int64_t* i_n, uint64_t A_truncate, uint64_t S_truncate,

@@ -109,6 +109,8 @@ def lib():
         L.oq_minimise.argtypes = [P, d, u64, u64, i32, i32, ctypes.POINTER(u64)]
         L.oq_minimise_nopassing.argtypes = [P, d, u64, u64, i32, ctypes.POINTER(u64)]
         L.oq_set_interaction_parameters.argtypes = [P, d, d]
+        L.oq_set_thermal.argtypes = [P, d, d, u64, u64, P, P, i32]
+        L.oq_get_thermal.argtypes = [P, pd]
         L.oq_minimise_truncate.argtypes = [P, P, u64, u64, d, u64, u64, i32, i32, ctypes.POINTER(u64)]
         L.oq_max_uniform_displacement.argtypes = [P, i32, pd]
         L.oq_event_driven_step.argtypes = [P, d, i32, i32, pd]
@@ -331,6 +333,12 @@ class System:
                                       int(max_iter_is_error), ctypes.byref(r)))
         return r.value
 
+    @property
+    def f_thermal(self):
+        out = np.empty(self.size)
+        self._check(lib().oq_get_thermal(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return out.reshape(self.shape)
+
     def minimise_nopassing(self, tol=1e-5, niter_tol=10, max_iter=int(1e9), max_iter_is_error=True):
         r = ctypes.c_uint64()
         self._check(lib().oq_minimise_nopassing(self._h, tol, niter_tol, int(max_iter), int(max_iter_is_error),
@@ -407,6 +415,58 @@ def line1d_longrange(m, eta, mu, k_interactions, alpha, k_frame, dt, shape, seed
     return System(CUSPY, LONGRANGE1D, shape=shape, m=m, eta=eta, mu=mu, k_interactions=k_interactions,
                   k_frame=k_frame, dt=dt, seed=seed, distribution=distribution, parameters=parameters,
                   interaction_parameters=(alpha, 0.0), **kw)
+
+
+PCG32_DEFAULT_STREAM = 0xDA3E39CB94B95BDB  # prrng's pcg32(seed) stream (pinned by the RandomForcing golden)
+_M64 = (1 << 64) - 1
+_PCG_MULT = 0x5851F42D4C957F2D
+
+
+def pcg32_seed(initstate, initseq=PCG32_DEFAULT_STREAM):
+    """(state, inc) of pcg32 seeded with (initstate, initseq) (the PCG seeding procedure)."""
+    inc = ((initseq << 1) | 1) & _M64
+    state = inc  # 0 * mult + inc
+    state = (state + initstate) & _M64
+    state = (state * _PCG_MULT + inc) & _M64
+    return state, inc
+
+
+def pcg32_randint(seed, n, high, initseq=PCG32_DEFAULT_STREAM):
+    """n draws in [0, high) as prrng.pcg32(seed).randint([n], high): the PCG bounded draw (reject
+    u32 below (2^32 - high) % high, then u32 % high).  Pinned with pcg32_seed's default stream by the
+    reference's RandomForcing golden trajectory."""
+    state, inc = pcg32_seed(seed, initseq)
+    thr = ((1 << 32) - high) % high
+    out = np.empty(n, dtype=np.int64)
+    i = 0
+    while i < n:
+        old = state
+        state = (old * _PCG_MULT + inc) & _M64
+        xs = (((old >> 18) ^ old) >> 27) & 0xFFFFFFFF
+        rot = old >> 59
+        r = ((xs >> rot) | (xs << ((-rot) & 31))) & 0xFFFFFFFF
+        if r >= thr:
+            out[i] = r % high
+            i += 1
+    return out
+
+
+def line1d_random_forcing(m, eta, mu, k_interactions, k_frame, dt, mean, stddev, seed_forcing, dinc_init, dinc,
+                          shape, seed, distribution, parameters, offset=-100.0, nchunk=5000, **kw):
+    """System_Cuspy_Laplace_RandomForcing (Line1d.h:264-330, RandomNormalForcing detail.h:881-1000):
+    every `dinc` increments (first at `dinc_init`) a particle's thermal force is redrawn from one pcg32
+    stream (seed_forcing, prrng's default stream), in particle order, as mean + stddev sqrt(2)
+    erfinv(2 r - 1), r = u32 2^-32."""
+    s = System(CUSPY, LAPLACE1D, shape=shape, m=m, eta=eta, mu=mu, k_interactions=k_interactions, k_frame=k_frame,
+               dt=dt, seed=seed, distribution=distribution, parameters=parameters, offset=offset, nchunk=nchunk,
+               **kw)
+    n = s.size
+    s._th_next = np.ascontiguousarray(np.broadcast_to(dinc_init, (n,)), dtype=np.int64)
+    s._th_dinc = np.ascontiguousarray(np.broadcast_to(dinc, (n,)), dtype=np.int64)
+    state, inc = pcg32_seed(int(seed_forcing))
+    s._check(lib().oq_set_thermal(s._h, float(mean), float(stddev), state, inc, s._th_next.ctypes.data,
+                                  s._th_dinc.ctypes.data, 0))
+    return s
 
 
 def line2d(**kw):

@@ -24,6 +24,8 @@ FILES = {
     "Line1d_Cuspy_Quartic": (1000, "x_frame"),
     "Line1d_Cuspy_Laplace_LongRange": (200, "x_frame"),
 }
+# third dataset "t_insta" (float) instead of "S" (int)
+THERMAL = {"Line1d_System_Cuspy_Laplace_RandomForcing": 500}
 
 
 def read(path: pathlib.Path, n: int, first: str):
@@ -45,6 +47,14 @@ def main():
         frame, f_frame, S = read(ref / "examples" / (stem + ".h5"), n, first)
         np.savez(out / (stem + ".npz"), frame=frame, f_frame=f_frame, S=S)
         print(stem, frame[-1], f_frame[-1], S.sum())
+    for stem, n in THERMAL.items():
+        raw = (ref / "examples" / (stem + ".h5")).read_bytes()
+        for name in ("x_frame", "f_frame", "t_insta"):
+            assert (name + "\x00").encode() in raw[:2048], (stem, name)
+        assert len(raw) == 2048 + 3 * 8 * n, (stem, len(raw))
+        cols = [np.frombuffer(raw[2048 + 8 * n * i: 2048 + 8 * n * (i + 1)], "<f8").copy() for i in range(3)]
+        np.savez(out / (stem + ".npz"), frame=cols[0], f_frame=cols[1], t_insta=cols[2])
+        print(stem, cols[0][-1], cols[1][-1], cols[2][-1])
 
 
 if __name__ == "__main__":
