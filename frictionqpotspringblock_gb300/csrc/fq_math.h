@@ -420,4 +420,123 @@ FQ_HD double fq_cos(double x)
     return fq_sin_shift(x, 1);
 }
 
+/* ---------------------------------------------------------------- erf / erfc / erfinv
+ * For the normal quantile of thermal forcing, mean + stddev sqrt(2) erfinv(2 r - 1).  erf by its
+ * Maclaurin series and erfc by its Laplace continued fraction, both in double-double; erfinv by Newton
+ * steps on those from Winitzki's closed-form approximation ("A handy approximation for the error
+ * function and its inverse", 2008).  Host and device run the same code, so they agree bit for bit.
+ */
+#define FQ_2_SQRTPI_HI 0x1.20dd750429b6dp+0
+#define FQ_2_SQRTPI_LO 0x1.1ae3a914fed80p-56
+#define FQ_1_SQRTPI_HI 0x1.20dd750429b6dp-1
+#define FQ_1_SQRTPI_LO 0x1.1ae3a914fed80p-57
+
+/* x / d for a double-double x and a double d. */
+FQ_HD fq_dd fq_dd_div_d(fq_dd x, double d)
+{
+    double q1 = FQ_DIV(x.hi, d);
+    fq_dd p = fq_two_prod(q1, d);
+    double r = FQ_ADD(FQ_SUB(FQ_SUB(x.hi, p.hi), p.lo), x.lo);
+    return fq_fast_two_sum(q1, FQ_DIV(r, d));
+}
+
+/* x / y for double-doubles (one correction step; y > 0 here). */
+FQ_HD fq_dd fq_dd_div(fq_dd x, fq_dd y)
+{
+    double q1 = FQ_DIV(x.hi, y.hi);
+    fq_dd r = fq_dd_add(x, fq_dd_neg(fq_dd_mul_d(y, q1)));
+    double q2 = FQ_DIV(r.hi, y.hi);
+    return fq_fast_two_sum(q1, q2);
+}
+
+/* exp of a double-double argument in [-745, 0], as a double-double (no rounding to double). */
+FQ_HD fq_dd fq_exp_dd_full(fq_dd P)
+{
+    double kf = FQ_MUL(P.hi, FQ_INV_LN2);
+    int n = (int)(kf >= 0.0 ? FQ_ADD(kf, 0.5) : FQ_SUB(kf, 0.5));
+    fq_dd r = fq_dd_add(P, fq_dd_neg(fq_dd_mul_d(fq_dd_make(FQ_LN2_HI, FQ_LN2_LO), (double)n)));
+    double ch, cl;
+    fq_inv_factorial(20, &ch, &cl);
+    fq_dd p = fq_dd_make(ch, cl);
+    for (int k = 19; k >= 0; --k) {
+        fq_inv_factorial(k, &ch, &cl);
+        p = fq_dd_add(fq_dd_mul(p, r), fq_dd_make(ch, cl));
+    }
+    const double sc = fq_pow2i(n < -1022 ? -1022 : n); /* the callers stay far above the subnormals */
+    return fq_dd_make(FQ_MUL(p.hi, sc), FQ_MUL(p.lo, sc));
+}
+
+/* erf(x), 0 <= x <= 2.5, double-double: (2/sqrt(pi)) sum_n (-1)^n x^(2n+1) / (n! (2n+1)). */
+FQ_HD fq_dd fq_erf_series(double x)
+{
+    const fq_dd x2 = fq_two_prod(x, x);
+    fq_dd t = fq_dd_make(x, 0.0); /* x^(2n+1) / n! */
+    fq_dd sum = t;
+    for (int n = 1; n < 120; ++n) {
+        t = fq_dd_div_d(fq_dd_mul(t, x2), (double)n);
+        fq_dd term = fq_dd_div_d(t, (double)(2 * n + 1));
+        sum = fq_dd_add(sum, (n & 1) ? fq_dd_neg(term) : term);
+        if (FQ_MUL(1e34, (term.hi < 0.0 ? -term.hi : term.hi)) < (sum.hi < 0.0 ? -sum.hi : sum.hi)) {
+            break;
+        }
+    }
+    return fq_dd_mul(sum, fq_dd_make(FQ_2_SQRTPI_HI, FQ_2_SQRTPI_LO));
+}
+
+/* erfc(x), x >= 0, double-double: 1 - erf below 2.5, the continued fraction
+ * erfc(x) = exp(-x^2) / (sqrt(pi) (x + (1/2) / (x + (2/2) / (x + (3/2) / ...)))) above (80 terms,
+ * evaluated from the tail). */
+FQ_HD fq_dd fq_erfc_dd(double x)
+{
+    if (x < 2.5) {
+        return fq_dd_add(fq_dd_make(1.0, 0.0), fq_dd_neg(fq_erf_series(x)));
+    }
+    fq_dd t = fq_dd_make(x, 0.0);
+    for (int k = 80; k >= 1; --k) {
+        t = fq_dd_add(fq_dd_make(x, 0.0), fq_dd_div(fq_dd_make(FQ_MUL(0.5, (double)k), 0.0), t));
+    }
+    fq_dd e = fq_exp_dd_full(fq_dd_neg(fq_two_prod(x, x)));
+    return fq_dd_div(fq_dd_mul(e, fq_dd_make(FQ_1_SQRTPI_HI, FQ_1_SQRTPI_LO)), t);
+}
+
+/* erfinv(y), -1 <= y <= 1. */
+FQ_HD double fq_erfinv(double y)
+{
+    if (y != y) {
+        return y;
+    }
+    const double a = y < 0.0 ? -y : y;
+    if (a > 1.0) {
+        return fq_from_bits(FQ_NAN_BITS);
+    }
+    if (a == 1.0) {
+        return y < 0.0 ? -fq_from_bits(FQ_INF_BITS) : fq_from_bits(FQ_INF_BITS);
+    }
+    if (a == 0.0) {
+        return y;
+    }
+    /* Winitzki: x^2 = sqrt(b^2 - ln(1 - a^2) / c) - b, b = 2 / (pi c) + ln(1 - a^2) / 2, c = 0.147 */
+    const double c = 0.147;
+    const double L = fq_log(FQ_MUL(FQ_SUB(1.0, a), FQ_ADD(1.0, a)));
+    const double b = FQ_ADD(FQ_DIV(0x1.45f306dc9c883p-1, c), FQ_MUL(0.5, L));
+    double x = FQ_SQRT(FQ_SUB(FQ_SQRT(FQ_SUB(FQ_MUL(b, b), FQ_DIV(L, c))), b));
+    const double q = FQ_SUB(1.0, a); /* exact for a >= 1/2 */
+    for (int it = 0; it < 6; ++it) {
+        /* Newton on erf(x) = a (small a) or erfc(x) = 1 - a (relative accuracy in the tail) */
+        const double d = FQ_MUL(FQ_2_SQRTPI_HI, fq_exp(-FQ_MUL(x, x)));
+        double r;
+        if (a <= 0.5) {
+            fq_dd e = fq_erf_series(x);
+            r = FQ_ADD(FQ_SUB(e.hi, a), e.lo);
+            x = FQ_SUB(x, FQ_DIV(r, d));
+        }
+        else {
+            fq_dd e = fq_erfc_dd(x);
+            r = FQ_ADD(FQ_SUB(e.hi, q), e.lo);
+            x = FQ_ADD(x, FQ_DIV(r, d));
+        }
+    }
+    return y < 0.0 ? -x : x;
+}
+
 #endif

@@ -158,6 +158,7 @@ double oq_math(int which, double x, double y, int math_mode)
         case 2: return m_sin(x, math_mode);
         case 3: return math_mode == OQ_MATH_PORTABLE ? fq_exp(x) : exp(x);
         case 4: return math_mode == OQ_MATH_PORTABLE ? fq_cos(x) : cos(x);
+        case 5: return fq_erfinv(x);
         default: return NAN;
     }
 }
@@ -566,48 +567,6 @@ static void compute_force(oq_system* s)
     }
 }
 
-/* inverse error function: a starting value refined by Newton steps on libm's erf (test tooling) */
-static double erfinv_d(double y)
-{
-    if (y <= -1.0) {
-        return -INFINITY;
-    }
-    if (y >= 1.0) {
-        return INFINITY;
-    }
-    double w = -log((1.0 - y) * (1.0 + y)), x;
-    if (w < 5.0) {
-        w -= 2.5;
-        x = 2.81022636e-08;
-        x = 3.43273939e-07 + x * w;
-        x = -3.5233877e-06 + x * w;
-        x = -4.39150654e-06 + x * w;
-        x = 0.00021858087 + x * w;
-        x = -0.00125372503 + x * w;
-        x = -0.00417768164 + x * w;
-        x = 0.246640727 + x * w;
-        x = 1.50140941 + x * w;
-    }
-    else {
-        w = sqrt(w) - 3.0;
-        x = -0.000200214257;
-        x = 0.000100950558 + x * w;
-        x = 0.00134934322 + x * w;
-        x = -0.00367342844 + x * w;
-        x = 0.00573950773 + x * w;
-        x = -0.0076224613 + x * w;
-        x = 0.00943887047 + x * w;
-        x = 1.00167406 + x * w;
-        x = 2.83297682 + x * w;
-    }
-    x *= y;
-    for (int i = 0; i < 4; ++i) {
-        double err = erf(x) - y;
-        x -= err / (1.1283791670955126 * exp(-x * x));
-    }
-    return x;
-}
-
 static double thermal_draw(oq_system* s)
 {
     uint64_t old = s->th_state;
@@ -616,7 +575,7 @@ static double thermal_draw(oq_system* s)
     uint32_t rot = (uint32_t)(old >> 59u);
     uint32_t u32 = (xs >> rot) | (xs << ((-rot) & 31));
     double r = (double)u32 * 0x1p-32;
-    double z = erfinv_d(2.0 * r - 1.0);
+    double z = fq_erfinv(2.0 * r - 1.0);
     if (s->th_mode == 1) {
         return s->th_mean + s->th_std * (M_SQRT2 * z);
     }

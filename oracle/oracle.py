@@ -140,7 +140,7 @@ def transform(distribution: str, parameters, r32: int, math_mode: int = MATH_POR
 
 
 def math(which: str, x: float, y: float = 0.0, math_mode: int = MATH_PORTABLE) -> float:
-    return lib().oq_math({"log": 0, "pow": 1, "sin": 2, "exp": 3, "cos": 4}[which], x, y, math_mode)
+    return lib().oq_math({"log": 0, "pow": 1, "sin": 2, "exp": 3, "cos": 4, "erfinv": 5}[which], x, y, math_mode)
 
 
 def sequence(seed, p, distribution, parameters, offset, nchunk, k0, count, math_mode=MATH_PORTABLE):

@@ -112,3 +112,19 @@ def test_cos_range():
         exact = float(mpmath.cos(mpmath.mpf(float(x))))
         worst = max(worst, ulp_diff(O.math("cos", float(x)), exact))
     assert worst <= 1
+
+
+def test_erfinv_correctly_rounded():
+    """fq_erfinv (the normal quantile of thermal forcing) against 40-digit erfinv on the inputs the
+    forcing produces, 2 r - 1 with r = u32 2^-32, and on edge values."""
+    mp = pytest.importorskip("mpmath")
+    mp.mp.dps = 40
+    rng = np.random.default_rng(7)
+    r = rng.integers(0, 2 ** 32, 4000, dtype=np.uint64).astype(np.float64) * 2.0 ** -32
+    ys = np.concatenate([2 * r - 1, [1e-300, -1e-20, 2.0 ** -52, 0.5, -0.5, 0.999999, 1 - 2.0 ** -31,
+                                     -(1 - 2.0 ** -32), 2.0 ** -31 - 1]])
+    for y in ys:
+        assert O.math("erfinv", float(y)) == float(mp.erfinv(mp.mpf(float(y)))), y
+    assert O.math("erfinv", 0.0) == 0.0
+    assert O.math("erfinv", 1.0) == np.inf and O.math("erfinv", -1.0) == -np.inf
+    assert np.isnan(O.math("erfinv", 1.5))
