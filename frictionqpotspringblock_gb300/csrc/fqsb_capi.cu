@@ -594,9 +594,8 @@ static int run(fqsb_system* h, int64_t max_steps, int flags, double tol, int64_t
             h->graph_np = nullptr;
         }
     }
-    const bool use_small = np == nullptr && h->small_ok && io == nullptr &&
-                           !(flags & (RF_SCHEDULE | RF_RECORD | RF_FFSUM)) &&
-                           !((flags & RF_RESID) && niter_tol > SMALL_RING_MAX);
+    bool use_small = np == nullptr && h->small_ok && io == nullptr && !(flags & (RF_SCHEDULE | RF_RECORD | RF_FFSUM)) &&
+                     !((flags & RF_RESID) && niter_tol > SMALL_RING_MAX);
     if (np) {
         if (h->use_graph && !h->graph_np) {
             CU(h, build_nopass_graph(h->d, h->lg, *np, &h->graph_np));
@@ -658,6 +657,7 @@ static int run(fqsb_system* h, int64_t max_steps, int flags, double tol, int64_t
                                                                     (long long*)&h->d.ctl->a_count);
         CU(h, cudaGetLastError());
     }
+    bool first_launch = true;
     for (;;) {
         if (np) {
             if (h->use_graph) {
@@ -672,7 +672,19 @@ static int run(fqsb_system* h, int64_t max_steps, int flags, double tol, int64_t
             }
         }
         else if (use_small) {
-            CU(h, launch_small_run(h->d, h->sg, h->stream));
+            cudaError_t le = launch_small_run(h->d, h->sg, h->stream);
+            if (first_launch && (le == cudaErrorInvalidClusterSize || le == cudaErrorLaunchOutOfResources)) {
+                /* the cluster could not be scheduled now (nothing ran): this handle uses the graph path */
+                cudaGetLastError();
+                h->small_ok = false;
+                use_small = false;
+                rc = ensure_graph(h);
+                if (rc) {
+                    return rc;
+                }
+                continue;
+            }
+            CU(h, le);
         }
         else if (h->use_graph) {
             CU(h, cudaGraphLaunch(h->graph, h->stream));
@@ -682,6 +694,7 @@ static int run(fqsb_system* h, int64_t max_steps, int flags, double tol, int64_t
                 CU(h, launch_iteration(h->d, h->lg, h->stream));
             }
         }
+        first_launch = false;
         CU(h, cudaMemcpyAsync(c, h->d.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, h->stream));
         rc = sync(h);
         if (rc) {
