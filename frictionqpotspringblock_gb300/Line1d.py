@@ -6,7 +6,7 @@ time-integration path: Cuspy, SemiSmooth and Smooth with Laplace1d interactions.
 """
 
 from . import _capi as C
-from ._system import System
+from ._system import System, _Hidden
 
 
 def version_dependencies():
@@ -107,16 +107,6 @@ class System_Cuspy_LongRange(System):
                          offset=offset, nchunk=nchunk, interaction_parameters=(alpha, 0.0), **kwargs)
 
 
-class _Hidden:
-    """A member of the base class that this class does not have (raises AttributeError, hasattr is False)."""
-
-    def __set_name__(self, owner, name):
-        self._name = name
-
-    def __get__(self, obj, objtype=None):
-        raise AttributeError(f"'{objtype.__name__}' object has no attribute '{self._name}'")
-
-
 class System_Cuspy_Laplace_Nopassing(System):
     """Cuspy + Laplace1d minimised with the no-passing rule, no dynamics (main.cpp:532-568, Line1d.h:173-238).
 
@@ -145,3 +135,46 @@ class System_Cuspy_Laplace_Nopassing(System):
         C.check(self._h, C.lib().fqsb_minimise_nopassing(self._h, float(tol), int(niter_tol), int(max_iter),
                                                           int(bool(max_iter_is_error)), C.ctypes.byref(out)))
         return out.value
+
+
+class _RandomForcing:
+    """Members of the RandomForcing systems: `external` (mySystemNdExternal, main.cpp:205-208); the
+    athermal members are absent as in the reference (its bindings omit mySystemNdAthermal)."""
+
+    external = property(lambda s: s._external, doc="Class adding external force")
+    minimise = _Hidden()
+    minimise_truncate = _Hidden()
+    eventDrivenStep = _Hidden()
+    quasistaticActivityFirst = _Hidden()
+    quasistaticActivityLast = _Hidden()
+
+
+class System_Cuspy_Laplace_RandomForcing(_RandomForcing, System):
+    """Cuspy + Laplace1d with a random normal force per particle, redrawn every `dinc` increments (first
+    at `dinc_init`) from one pcg32 stream (main.cpp:570-621, Line1d.h:264-330, detail.h:881-1000)."""
+
+    _potential = C.CUSPY
+    _interactions = C.LAPLACE1D
+    _rank = 1
+    _name = "Line1d.System_Cuspy_Laplace_RandomForcing"
+
+    def __init__(self, m, eta, mu, k_interactions, k_frame, dt, mean, stddev, seed_forcing, dinc_init, dinc, shape,
+                 seed, distribution, parameters, offset=-100.0, nchunk=5000, **kwargs):
+        super().__init__(m, eta, mu, k_interactions, k_frame, dt, shape, seed, distribution, parameters,
+                         offset=offset, nchunk=nchunk, **kwargs)
+        self._attach_random_forcing(mean, stddev, seed_forcing, dinc_init, dinc)
+
+
+class System_Cuspy_Quartic_RandomForcing(_RandomForcing, System):
+    """Cuspy + Quartic1d with a random normal force per particle (main.cpp:623-676, Line1d.h:486-556)."""
+
+    _potential = C.CUSPY
+    _interactions = C.QUARTIC1D
+    _rank = 1
+    _name = "Line1d.System_Cuspy_Quartic_RandomForcing"
+
+    def __init__(self, m, eta, mu, a1, a2, k_frame, dt, mean, stddev, seed_forcing, dinc_init, dinc, shape, seed,
+                 distribution, parameters, offset=-100.0, nchunk=5000, **kwargs):
+        super().__init__(m, eta, mu, 0.0, k_frame, dt, shape, seed, distribution, parameters, offset=offset,
+                         nchunk=nchunk, interaction_parameters=(a1, a2), **kwargs)
+        self._attach_random_forcing(mean, stddev, seed_forcing, dinc_init, dinc)

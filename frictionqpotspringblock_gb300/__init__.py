@@ -9,7 +9,7 @@ Every call goes through the C ABI of libfqsb.so (include/fqsb.h) to FP64
 kernels for sm_103a; there is no CPU fallback.
 """
 
-from . import Line1d, Line2d, Particles  # noqa: F401
+from . import Line1d, Line2d, Particles, detail  # noqa: F401
 from ._capi import FrictionError  # noqa: F401
 
 __version__ = "0.1.0"

@@ -137,6 +137,9 @@ SIGNATURES = [
     ("fqsb_get_stream", _I, [_P, ctypes.POINTER(_P)]),
     ("fqsb_residual_noalloc", _I, [_P, _P, _I64, _P, _P]),
     ("fqsb_set_parameters", _I, [_P, _D, _D, _D]),
+    ("fqsb_set_random_forcing", _I, [_P, _D, _D, _U64, _PI64, _PI64]),
+    ("fqsb_random_forcing_get", _I, [_P, _PU64, _PD, _PI64]),
+    ("fqsb_random_forcing_set", _I, [_P, _PU64, _PD, _PI64]),
     ("fqsb_adjoint_forward", _I, [_P, _PD, _I64, _I64, _I64, _PD]),
     ("fqsb_adjoint_backward", _I, [_P, _PD, _PD, _PD, _PD]),
     ("fqsb_batch_create", _I, [ctypes.POINTER(BatchConfig), ctypes.POINTER(_P)]),

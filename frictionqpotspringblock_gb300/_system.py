@@ -91,6 +91,76 @@ class Chunk:
                                                  _ptr(idx, ctypes.c_int64)))
 
 
+class RandomNormalForcing:
+    """Proxy of `system.external` of the RandomForcing systems (detail.RandomNormalForcing_1,
+    main.cpp:251-275, detail.h:881-1000): the pcg32 state of the draws, the current thermal forces and
+    the increment of each particle's next draw.  Getters return copies; setters write through."""
+
+    def __init__(self, system: "System"):
+        self._s = system
+
+    def __repr__(self):
+        return "<FrictionQPotSpringBlock.detail.RandomNormalForcing_1>"
+
+    @property
+    def state(self) -> int:
+        """State of RNG"""
+        s = self._s
+        out = ctypes.c_uint64()
+        C.check(s._h, C.lib().fqsb_random_forcing_get(s._h, ctypes.byref(out), None, None))
+        return out.value
+
+    @state.setter
+    def state(self, value):
+        s = self._s
+        st = ctypes.c_uint64(int(value))
+        C.check(s._h, C.lib().fqsb_random_forcing_set(s._h, ctypes.byref(st), None, None))
+
+    @property
+    def f_thermal(self) -> np.ndarray:
+        """Random force"""
+        s = self._s
+        out = np.empty(s.size)
+        C.check(s._h, C.lib().fqsb_random_forcing_get(s._h, None, _ptr(out, ctypes.c_double), None))
+        return out.reshape(s.shape)
+
+    @f_thermal.setter
+    def f_thermal(self, value):
+        s = self._s
+        arr = np.ascontiguousarray(value, dtype=np.float64)
+        if list(arr.shape) != s.shape:
+            raise RuntimeError("assertion failed (xt::has_shape(f_thermal, m_f_thermal.shape()))")
+        arr = arr.ravel()
+        C.check(s._h, C.lib().fqsb_random_forcing_set(s._h, None, _ptr(arr, ctypes.c_double), None))
+
+    @property
+    def next(self) -> np.ndarray:
+        """Next draw increment"""
+        s = self._s
+        out = np.empty(s.size, np.int64)
+        C.check(s._h, C.lib().fqsb_random_forcing_get(s._h, None, None, _ptr(out, ctypes.c_int64)))
+        return out.reshape(s.shape)
+
+    @next.setter
+    def next(self, value):
+        s = self._s
+        arr = np.ascontiguousarray(value, dtype=np.int64)
+        if list(arr.shape) != s.shape:
+            raise RuntimeError("assertion failed (xt::has_shape(next, m_next.shape()))")
+        arr = arr.ravel()
+        C.check(s._h, C.lib().fqsb_random_forcing_set(s._h, None, None, _ptr(arr, ctypes.c_int64)))
+
+
+class _Hidden:
+    """A member of the base class that this class does not have (raises AttributeError, hasattr is False)."""
+
+    def __set_name__(self, owner, name):
+        self._name = name
+
+    def __get__(self, obj, objtype=None):
+        raise AttributeError(f"'{objtype.__name__}' object has no attribute '{self._name}'")
+
+
 class System:
     """A system resident on the GPU.  Concrete classes fix the potential and the interactions."""
 
@@ -142,6 +212,15 @@ class System:
         self._nchunk = int(nchunk)
         self._dt, self._mu, self._eta, self._m, self._k_frame = float(dt), float(mu), float(eta), float(m), float(k_frame)
         self._chunk = Chunk(self)
+
+    def _attach_random_forcing(self, mean, stddev, seed_forcing, dinc_init, dinc):
+        """RandomNormalForcing of the RandomForcing systems (detail.h:903-919), attached at construction."""
+        self._th_next0 = np.ascontiguousarray(np.broadcast_to(np.asarray(dinc_init), self._shape), dtype=np.int64)
+        self._th_dinc = np.ascontiguousarray(np.broadcast_to(np.asarray(dinc), self._shape), dtype=np.int64)
+        C.check(self._h, C.lib().fqsb_set_random_forcing(self._h, float(mean), float(stddev), int(seed_forcing),
+                                                          _ptr(self._th_next0.ravel(), ctypes.c_int64),
+                                                          _ptr(self._th_dinc.ravel(), ctypes.c_int64)))
+        self._external = RandomNormalForcing(self)
 
     def __del__(self):
         h = getattr(self, "_h", None)

@@ -153,6 +153,12 @@ __device__ __forceinline__ void pi_force(const DevSys& d, const double* u, int64
     fi = inter_force_at(d, u, p);
 }
 
+/* computeForce with External (detail.h:1326-1328): the thermal force is the last term of the sum */
+__device__ __forceinline__ double with_f_thermal(const DevSys& d, int64_t p, double f)
+{
+    return d.f_th ? FQ_ADD(f, d.f_th[p]) : f;
+}
+
 /* all force components of particle p from the state (u, v, u_frame) */
 __device__ __forceinline__ void all_forces(const DevSys& d, const double* u, const double* v, double uf, int64_t p,
                                            double* out5)
@@ -165,7 +171,7 @@ __device__ __forceinline__ void all_forces(const DevSys& d, const double* u, con
     out5[1] = fi;
     out5[2] = ff;
     out5[3] = fd;
-    out5[4] = FQ_ADD(FQ_ADD(FQ_ADD(ff, fp), fi), fd);
+    out5[4] = with_f_thermal(d, p, FQ_ADD(FQ_ADD(FQ_ADD(ff, fp), fi), fd));
 }
 
 __global__ void k_forces(DevSys d, const double* u, const double* v, double uf, double* fpot, double* fint,
@@ -192,7 +198,7 @@ __global__ void k_store_frame(DevSys d, const double* u, double uf, double* fs0,
     if (p < d.N) {
         double ff = FQ_MUL(d.k_frame, FQ_SUB(uf, u[p]));
         fs2[p] = ff;
-        fs4[p] = FQ_ADD(FQ_ADD(FQ_ADD(ff, fs0[p]), fs1[p]), fs3[p]);
+        fs4[p] = with_f_thermal(d, p, FQ_ADD(FQ_ADD(FQ_ADD(ff, fs0[p]), fs1[p]), fs3[p]));
     }
 }
 
@@ -204,7 +210,7 @@ __global__ void k_store_damp(DevSys d, const double* v, double* fs0, double* fs1
     if (p < d.N) {
         double fd = FQ_MUL(d.me, v[p]);
         fs3[p] = fd;
-        fs4[p] = FQ_ADD(FQ_ADD(FQ_ADD(fs2[p], fs0[p]), fs1[p]), fd);
+        fs4[p] = with_f_thermal(d, p, FQ_ADD(FQ_ADD(FQ_ADD(fs2[p], fs0[p]), fs1[p]), fd));
     }
 }
 
@@ -758,7 +764,8 @@ static void free_all(fqsb_system* h)
     DevSys& d = h->d;
     void* ptrs[] = {d.data, d.start, d.cidx, d.gidx, d.wc, d.acc_end, d.anc_kind, d.anc_k, d.anc_state, d.anc_val,
                     d.u[0], d.u[1], d.v[0], d.v[1], d.a[0], d.a[1], d.ctl, d.ring, d.partials, d.i_n, d.sq2,
-                    d.cta_pending, d.regen_list, (void*)d.lr_pref,
+                    d.cta_pending, d.regen_list, (void*)d.lr_pref, d.f_th, d.th_next, (void*)d.th_dinc, d.th_cnt,
+                    d.th,
                     (void*)d.offp, h->scratch, h->red_partials, h->red_out, h->mkey, h->mflag, h->fs[0], h->fs[1],
                     h->fs[2], h->fs[3], h->fs[4], h->adj_sched, h->adj_ckpt, h->adj_ffsum, h->adj_final};
     for (void* p : ptrs) {
@@ -1171,9 +1178,9 @@ extern "C" int fqsb_minimise_nopassing(fqsb_system* h, double tol, uint64_t nite
     if (!(tol < 1.0)) {
         return set_err(h, FQSB_ERR_INVALID, "assertion failed (tol < 1.0)");
     }
-    if (h->d.pot != POT_CUSPY || h->d.inter != INTER_LAPLACE1D || h->d.N < 2) {
+    if (h->d.pot != POT_CUSPY || h->d.inter != INTER_LAPLACE1D || h->d.N < 2 || h->d.f_th) {
         return set_err(h, FQSB_ERR_INVALID,
-                       "the no-passing minimiser needs the Cuspy potential on a Line1d ring, N >= 2");
+                       "the no-passing minimiser needs the athermal Cuspy potential on a Line1d ring, N >= 2");
     }
     for (int i = 0; i < 5; ++i) {
         if (!h->fs[i]) {
@@ -1379,13 +1386,168 @@ extern "C" int fqsb_quench(fqsb_system* h)
     return rc ? rc : sync(h);
 }
 
+/* updated_inc (detail.h:1369-1375): thermal draws at the current inc, then computeForce */
+static int updated_inc(fqsb_system* h)
+{
+    if (!h->d.f_th) {
+        return FQSB_OK;
+    }
+    CU(h, launch_thermal_draw(h->d, 0, h->inc, h->stream));
+    if (h->stored) {
+        /* f from the stored components (f_damping is -eta v in the store) and the new f_thermal */
+        k_store_damp<<<blocks_for(h->d.N, 128), 128, 0, h->stream>>>(h->d, cur_v(h), h->fs[0], h->fs[1], h->fs[2],
+                                                                    h->fs[3], h->fs[4]);
+        CU(h, cudaGetLastError());
+    }
+    return FQSB_OK;
+}
+
+/* refresh detail.h:1310-1315: updated_u, updated_v, updated_inc */
 extern "C" int fqsb_refresh(fqsb_system* h)
 {
     if (!h) {
         return FQSB_ERR_INVALID;
     }
     int rc = updated_u(h);
+    if (!rc) {
+        rc = updated_inc(h);
+    }
     return rc ? rc : sync(h);
+}
+
+/* ------------------------------------------------------------ thermal forcing */
+
+extern "C" int fqsb_set_random_forcing(fqsb_system* h, double mean, double stddev, uint64_t seed,
+                                       const int64_t* dinc_init, const int64_t* dinc)
+{
+    if (!h || !dinc_init || !dinc) {
+        return FQSB_ERR_INVALID;
+    }
+    DevSys& d = h->d;
+    if (d.f_th) {
+        return set_err(h, FQSB_ERR_INVALID, "the system already has a RandomNormalForcing");
+    }
+    if (d.pot != POT_CUSPY || !(d.inter == INTER_LAPLACE1D || d.inter == INTER_QUARTIC1D || d.inter == INTER_NONE)) {
+        return set_err(h, FQSB_ERR_UNSUPPORTED,
+                       "RandomNormalForcing is implemented for the Cuspy potential with Laplace1d, Quartic1d or no "
+                       "interactions");
+    }
+    const int64_t N = d.N;
+    const int64_t G = thermal_tiles(N);
+    double* f_th = nullptr;
+    int64_t *next = nullptr, *di = nullptr, *cnt = nullptr;
+    Thermal* th = nullptr;
+    cudaError_t e = cudaMalloc(&f_th, sizeof(double) * (size_t)padded(N));
+    if (e == cudaSuccess) {
+        e = cudaMalloc(&next, sizeof(int64_t) * (size_t)N);
+    }
+    if (e == cudaSuccess) {
+        e = cudaMalloc(&di, sizeof(int64_t) * (size_t)N);
+    }
+    if (e == cudaSuccess) {
+        e = cudaMalloc(&cnt, sizeof(int64_t) * (size_t)G);
+    }
+    if (e == cudaSuccess) {
+        e = cudaMalloc(&th, sizeof(Thermal));
+    }
+    /* prrng pcg32(seed): the PCG seeding procedure on the default stream */
+    Thermal t0;
+    t0.inc = (PCG_DEFAULT_STREAM << 1u) | 1u;
+    t0.state = 0u;
+    t0.state = t0.state * PCG_MULT + t0.inc;
+    t0.state += seed;
+    t0.state = t0.state * PCG_MULT + t0.inc;
+    t0.base = t0.state;
+    t0.ticket = 0u;
+    t0.pad = 0u;
+    if (e == cudaSuccess) {
+        e = cudaMemsetAsync(f_th, 0, sizeof(double) * (size_t)padded(N), h->stream);
+    }
+    if (e == cudaSuccess) {
+        e = cudaMemcpyAsync(next, dinc_init, sizeof(int64_t) * (size_t)N, cudaMemcpyHostToDevice, h->stream);
+    }
+    if (e == cudaSuccess) {
+        e = cudaMemcpyAsync(di, dinc, sizeof(int64_t) * (size_t)N, cudaMemcpyHostToDevice, h->stream);
+    }
+    if (e == cudaSuccess) {
+        e = cudaMemcpyAsync(th, &t0, sizeof(Thermal), cudaMemcpyHostToDevice, h->stream);
+    }
+    if (e == cudaSuccess) {
+        e = cudaStreamSynchronize(h->stream);
+    }
+    if (e != cudaSuccess) {
+        for (void* q : {(void*)f_th, (void*)next, (void*)di, (void*)cnt, (void*)th}) {
+            if (q) {
+                cudaFree(q);
+            }
+        }
+        return set_err(h, FQSB_ERR_CUDA, std::string("RandomNormalForcing allocation failed: ") + cudaGetErrorString(e));
+    }
+    d.f_th = f_th;
+    d.th_next = next;
+    d.th_dinc = di;
+    d.th_cnt = cnt;
+    d.th = th;
+    d.th_mean = mean;
+    d.th_sc = stddev * M_SQRT2; /* the association of the reference's normal transform */
+    /* the run graph's kernels take the new pointers; the one-cluster kernel has no thermal term */
+    if (h->graph) {
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;
+    }
+    h->small_ok = false;
+    int rc = updated_inc(h); /* the constructor's refresh */
+    return rc ? rc : sync(h);
+}
+
+extern "C" int fqsb_random_forcing_get(fqsb_system* h, uint64_t* state, double* f_thermal, int64_t* next)
+{
+    if (!h) {
+        return FQSB_ERR_INVALID;
+    }
+    if (!h->d.f_th) {
+        return set_err(h, FQSB_ERR_INVALID, "the system has no RandomNormalForcing");
+    }
+    if (state) {
+        CU(h, cudaMemcpyAsync(state, &h->d.th->state, sizeof(uint64_t), cudaMemcpyDeviceToHost, h->stream));
+    }
+    if (f_thermal) {
+        CU(h, cudaMemcpyAsync(f_thermal, h->d.f_th, sizeof(double) * (size_t)h->d.N, cudaMemcpyDeviceToHost,
+                              h->stream));
+    }
+    if (next) {
+        CU(h, cudaMemcpyAsync(next, h->d.th_next, sizeof(int64_t) * (size_t)h->d.N, cudaMemcpyDeviceToHost,
+                              h->stream));
+    }
+    return sync(h);
+}
+
+extern "C" int fqsb_random_forcing_set(fqsb_system* h, const uint64_t* state, const double* f_thermal,
+                                       const int64_t* next)
+{
+    if (!h) {
+        return FQSB_ERR_INVALID;
+    }
+    if (!h->d.f_th) {
+        return set_err(h, FQSB_ERR_INVALID, "the system has no RandomNormalForcing");
+    }
+    if (state) {
+        CU(h, cudaMemcpyAsync(&h->d.th->state, state, sizeof(uint64_t), cudaMemcpyHostToDevice, h->stream));
+    }
+    if (f_thermal) {
+        /* set_f_thermal (detail.h:972-976) does not recompute f: keep the forces of before */
+        int rc = materialise_forces(h);
+        if (rc) {
+            return rc;
+        }
+        CU(h, cudaMemcpyAsync(h->d.f_th, f_thermal, sizeof(double) * (size_t)h->d.N, cudaMemcpyHostToDevice,
+                              h->stream));
+    }
+    if (next) {
+        CU(h, cudaMemcpyAsync(h->d.th_next, next, sizeof(int64_t) * (size_t)h->d.N, cudaMemcpyHostToDevice,
+                              h->stream));
+    }
+    return sync(h);
 }
 
 /* ------------------------------------------------------------ state */
@@ -1559,6 +1721,10 @@ extern "C" int fqsb_set_inc(fqsb_system* h, int64_t inc)
     h->inc = inc;
     h->qs_first = inc;
     h->qs_last = inc;
+    if (h->d.f_th) {
+        int rc = updated_inc(h); /* set_inc detail.h:1241-1247 */
+        return rc ? rc : sync(h);
+    }
     return FQSB_OK;
 }
 
@@ -1769,9 +1935,9 @@ extern "C" int fqsb_adjoint_forward(fqsb_system* h, const double* schedule, int6
         return FQSB_ERR_INVALID;
     }
     if (h->is2d || h->d.inter == INTER_QUARTIC1D || h->d.inter == INTER_QUARTICGRAD1D ||
-        h->d.inter == INTER_LONGRANGE1D) {
+        h->d.inter == INTER_LONGRANGE1D || h->d.f_th) {
         return set_err(h, FQSB_ERR_UNSUPPORTED,
-                       "the adjoint is implemented for Line1d (Laplace1d) and Particles systems");
+                       "the adjoint is implemented for athermal Line1d (Laplace1d) and Particles systems");
     }
     int64_t N = h->d.N;
     int64_t nseg = (T + K - 1) / K;

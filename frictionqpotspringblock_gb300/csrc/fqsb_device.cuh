@@ -124,6 +124,39 @@ struct Ctl {
     double* rec_ffsum;
 };
 
+/*
+ * RandomNormalForcing (detail.h:881-1000): the pcg32 stream all draws come from, in particle order
+ * (prrng's pcg32 m_state / m_inc), and the bookkeeping of one draw: the state before it (base) and
+ * the ticket of its counting kernel.
+ */
+struct Thermal {
+    uint64_t state;
+    uint64_t inc;
+    uint64_t base;
+    uint32_t ticket;
+    uint32_t pad;
+};
+
+/* prrng pcg32(seed): the PCG seeding procedure on the default stream 0xda3e39cb94b95bdb */
+constexpr uint64_t PCG_DEFAULT_STREAM = 0xda3e39cb94b95bdbULL;
+
+/* LCG jump-ahead of a pcg32 stream with increment `inc` by delta steps (mod 2^64), Brown (1994),
+ * "Random number generation with arbitrary strides". */
+__host__ __device__ inline uint64_t pcg_advance_inc(uint64_t state, uint64_t delta, uint64_t inc)
+{
+    uint64_t cur_mult = PCG_MULT, cur_plus = inc, acc_mult = 1ULL, acc_plus = 0ULL;
+    while (delta > 0) {
+        if (delta & 1ULL) {
+            acc_mult *= cur_mult;
+            acc_plus = acc_plus * cur_mult + cur_plus;
+        }
+        cur_plus = (cur_mult + 1ULL) * cur_plus;
+        cur_mult *= cur_mult;
+        delta >>= 1u;
+    }
+    return acc_mult * state + acc_plus;
+}
+
 /* How a multiplication by a positive parameter c is carried out (all exact-equivalent to x * c). */
 enum : int { SCALE_ONE = 0, SCALE_POW2 = 1, SCALE_GENERAL = 2 };
 
@@ -178,6 +211,13 @@ struct DevSys {
     unsigned long long h_while; /* cudaGraphConditionalHandle of the run loop */
     unsigned long long h_if;    /* cudaGraphConditionalHandle of the regeneration branch */
     int in_graph;               /* 0: kernels launched one by one by the host (no conditional handles) */
+    /* RandomNormalForcing (f_th == NULL: none) */
+    double* f_th;       /* f_thermal [N] */
+    int64_t* th_next;   /* next increment at which particle p redraws */
+    const int64_t* th_dinc;
+    int64_t* th_cnt;    /* per 1024-particle tile: draws, then their exclusive prefix */
+    Thermal* th;
+    double th_mean, th_sc; /* mean and stddev * sqrt(2) (rounded as the reference's normal transform) */
 };
 
 /* ------------------------------------------------------------ pcg32 */

@@ -59,6 +59,11 @@ static const int NOPASS_MAX_REALIGN = 1 << 20; /* bound on one particle's well u
 cudaError_t build_nopass_graph(const DevSys& s, const LineGeom& g, const NopassArgs& A, cudaGraphExec_t* exec);
 cudaError_t launch_nopass_iteration(const DevSys& s, const LineGeom& g, const NopassArgs& A, cudaStream_t st);
 
+/* RandomNormalForcing draw (updated_inc): from_ctl = 1 for the step a run is about to make (inside
+ * the run loop), else at increment `inc`.  thermal_tiles: size of DevSys::th_cnt. */
+cudaError_t launch_thermal_draw(const DevSys& s, int from_ctl, int64_t inc, cudaStream_t st);
+int64_t thermal_tiles(int64_t N);
+
 /* One loop iteration launched kernel by kernel by the host (s.in_graph must be 0). */
 cudaError_t launch_iteration(const DevSys& s, const LineGeom& g, cudaStream_t st);
 

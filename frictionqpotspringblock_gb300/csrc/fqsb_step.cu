@@ -60,19 +60,27 @@ __device__ __forceinline__ double u_next(const DevSys& s, const double* u0, cons
     return S_ADD(3, S_ADD(2, u0[q], S_MUL(0, s.dt, v0[q])), S_MUL(1, s.hdt2, a0[q]));
 }
 
-/* velocity / acceleration updates of timeStep after the positions, detail.h:1552-1565 */
-template <unsigned SOFT = 0u>
+/* f = (sfi + f_damping) [+ f_thermal]: computeForce, detail.h:1321-1330 */
+template <bool TH>
+__device__ __forceinline__ double with_thermal(double f, double fth)
+{
+    return TH ? __dadd_rn(f, fth) : f;
+}
+
+/* velocity / acceleration updates of timeStep after the positions, detail.h:1552-1565 (TH: with the
+ * thermal force of RandomNormalForcing as the last term of each force sum) */
+template <unsigned SOFT = 0u, bool TH = false>
 __device__ __forceinline__ void verlet_velocity(const DevSys& s, double sfi, double v0, double a0, double& v, double& a,
-                                                double& f)
+                                                double& f, double fth = 0.0)
 {
     v = S_ADD(11, v0, S_MUL(10, s.dt, a0));
-    f = S_ADD(13, sfi, S_MUL(12, s.me, v));
+    f = with_thermal<TH>(S_ADD(13, sfi, S_MUL(12, s.me, v)), fth);
     a = scale(f, s.s_im);
     v = S_ADD(16, v0, S_MUL(15, s.hdt, S_ADD(14, a0, a)));
-    f = S_ADD(18, sfi, S_MUL(17, s.me, v));
+    f = with_thermal<TH>(S_ADD(18, sfi, S_MUL(17, s.me, v)), fth);
     a = scale(f, s.s_im);
     v = S_ADD(21, v0, S_MUL(20, s.hdt, S_ADD(19, a0, a)));
-    f = S_ADD(23, sfi, S_MUL(22, s.me, v));
+    f = with_thermal<TH>(S_ADD(23, sfi, S_MUL(22, s.me, v)), fth);
     a = scale(f, s.s_im);
 }
 
@@ -447,7 +455,7 @@ __device__ __forceinline__ void step_epilogue(const DevSys& s, StepShared& sh, i
  * from the old state.  State arrays are padded to a multiple of 1024 entries.  redo = 1: only CTAs
  * marked pending run (after k_regen moved their particles' windows).
  */
-template <int POT, int INTER, int PPT, unsigned SOFT = STEP_SOFT>
+template <int POT, int INTER, int PPT, unsigned SOFT = STEP_SOFT, bool TH = false>
 __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_line(DevSys s, int redo)
 {
     __shared__ StepShared sh;
@@ -535,7 +543,7 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_line(DevSys s
         }
         double sfi = S_ADD(9, sfp, fi);
         double f;
-        verlet_velocity<SOFT>(s, sfi, vr[j], ar[j], vo[j], ao[j], f);
+        verlet_velocity<SOFT, TH>(s, sfi, vr[j], ar[j], vo[j], ao[j], f, TH ? s.f_th[p] : 0.0);
         nan |= is_nan_bits(up);
         if (resid) {
             /* squares on the integer pipes (bit-identical), sums on the fp64 pipe */
@@ -764,6 +772,172 @@ __global__ void __launch_bounds__(128) k_regen(DevSys s)
             atomicAdd((unsigned long long*)&c->a_count, (unsigned long long)da);
         }
     }
+}
+
+/* ------------------------------------------------------------- thermal forcing */
+
+/*
+ * RandomNormalForcing::force (detail.h:930-942), run by updated_inc at the start of every time step
+ * (timeStep :1540-1544) and by refresh / set_inc: in particle order, every particle with inc >= next[p]
+ * takes the next draw of one pcg32 stream, f_thermal[p] = mean + (stddev sqrt 2) erfinv(2 r - 1)
+ * (r = u32 2^-32), and next[p] += dinc[p].  The draws are numbered by an exclusive scan over the flat
+ * index: k_th_count counts each 1024-particle tile's draws and its last CTA turns the counts into
+ * tile offsets and jumps the stream past the whole draw; k_th_draw gives the particle with rank k
+ * the k-th output after the old state (one jump per thread, then single steps), so the result equals
+ * the reference's sequential loop.
+ *
+ * from_ctl = 1: inside a run, for the step about to run (inc = Ctl::inc + 1); nothing happens once the
+ * run is over or when the run's iterations are not time steps.  from_ctl = 0: at inc = inc_arg.
+ */
+constexpr int TH_TILE = 1024; /* particles per CTA of the draw kernels: 256 threads x 4 */
+
+__device__ __forceinline__ bool th_draw_inc(const DevSys& s, int from_ctl, int64_t inc_arg, int64_t& inc)
+{
+    if (!from_ctl) {
+        inc = inc_arg;
+        return true;
+    }
+    volatile Ctl* c = s.ctl;
+    if (c->done || c->error || (c->flags & RF_NOINC)) {
+        return false;
+    }
+    inc = c->inc + 1;
+    return true;
+}
+
+/* Exclusive prefix of x over the CTA's 256 threads (8 warps); *total gets the CTA's sum. */
+__device__ __forceinline__ int64_t cta_exclusive_scan256(int64_t x, int64_t* sh8, int64_t* total)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int64_t incl = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int64_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) {
+            incl += y;
+        }
+    }
+    if (lane == 31) {
+        sh8[warp] = incl;
+    }
+    __syncthreads();
+    int64_t before = 0, all = 0;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) {
+        int64_t t = sh8[w];
+        before += w < warp ? t : 0;
+        all += t;
+    }
+    __syncthreads();
+    *total = all;
+    return before + incl - x;
+}
+
+__global__ void __launch_bounds__(256) k_th_count(DevSys s, int from_ctl, int64_t inc_arg)
+{
+    __shared__ int64_t sh8[8];
+    __shared__ int sh_last;
+    int64_t inc;
+    if (!th_draw_inc(s, from_ctl, inc_arg, inc)) {
+        return;
+    }
+    const int64_t p0 = (int64_t)blockIdx.x * TH_TILE + (int64_t)threadIdx.x * 4;
+    int64_t n = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        int64_t p = p0 + j;
+        n += (p < s.N && inc >= s.th_next[p]) ? 1 : 0;
+    }
+    int64_t tile_total;
+    cta_exclusive_scan256(n, sh8, &tile_total);
+    if (threadIdx.x == 0) {
+        s.th_cnt[blockIdx.x] = tile_total;
+        __threadfence();
+        unsigned t = atomicAdd(&s.th->ticket, 1u);
+        sh_last = (t == gridDim.x - 1u) ? 1 : 0;
+    }
+    __syncthreads();
+    if (!sh_last) {
+        return;
+    }
+    /* last CTA: tile counts -> exclusive tile offsets (in place), the stream jumps past all draws */
+    __threadfence();
+    const int64_t G = gridDim.x;
+    const int64_t per = (G + 255) / 256;
+    const int64_t lo = (int64_t)threadIdx.x * per;
+    const int64_t hi = lo + per < G ? lo + per : G;
+    int64_t sum = 0;
+    for (int64_t i = lo; i < hi; ++i) {
+        sum += __ldcg(s.th_cnt + i);
+    }
+    int64_t all;
+    int64_t run = cta_exclusive_scan256(sum, sh8, &all);
+    for (int64_t i = lo; i < hi; ++i) {
+        int64_t x = __ldcg(s.th_cnt + i);
+        s.th_cnt[i] = run;
+        run += x;
+    }
+    if (threadIdx.x == 0) {
+        Thermal* th = s.th;
+        uint64_t base = th->state;
+        th->base = base;
+        th->state = pcg_advance_inc(base, (uint64_t)all, th->inc);
+        th->ticket = 0u;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_th_draw(DevSys s, int from_ctl, int64_t inc_arg)
+{
+    __shared__ int64_t sh8[8];
+    int64_t inc;
+    if (!th_draw_inc(s, from_ctl, inc_arg, inc)) {
+        return;
+    }
+    const int64_t p0 = (int64_t)blockIdx.x * TH_TILE + (int64_t)threadIdx.x * 4;
+    bool draw[4];
+    int64_t n = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        int64_t p = p0 + j;
+        draw[j] = p < s.N && inc >= s.th_next[p];
+        n += draw[j] ? 1 : 0;
+    }
+    int64_t tile_total;
+    const int64_t k = s.th_cnt[blockIdx.x] + cta_exclusive_scan256(n, sh8, &tile_total);
+    if (n == 0) {
+        return;
+    }
+    const uint64_t sinc = s.th->inc;
+    uint64_t st = pcg_advance_inc(s.th->base, (uint64_t)k, sinc); /* state before draw number k */
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        if (!draw[j]) {
+            continue;
+        }
+        int64_t p = p0 + j;
+        uint32_t u32 = pcg_output(st);
+        st = st * PCG_MULT + sinc;
+        double r = FQ_MUL((double)u32, 0x1p-32);
+        double z = fq_erfinv(FQ_SUB(FQ_MUL(2.0, r), 1.0));
+        s.f_th[p] = FQ_ADD(s.th_mean, FQ_MUL(s.th_sc, z));
+        s.th_next[p] += s.th_dinc[p];
+    }
+}
+
+cudaError_t launch_thermal_draw(const DevSys& s, int from_ctl, int64_t inc, cudaStream_t st)
+{
+    unsigned G = (unsigned)((s.N + TH_TILE - 1) / TH_TILE);
+    void* args[] = {(void*)&s, (void*)&from_ctl, (void*)&inc};
+    cudaError_t e = cudaLaunchKernel((void*)k_th_count, dim3(G), dim3(256), args, 0, st);
+    if (e == cudaSuccess) {
+        e = cudaLaunchKernel((void*)k_th_draw, dim3(G), dim3(256), args, 0, st);
+    }
+    return e;
+}
+
+int64_t thermal_tiles(int64_t N)
+{
+    return (N + TH_TILE - 1) / TH_TILE;
 }
 
 /* ------------------------------------------------------------- long-range interactions */
@@ -1366,14 +1540,22 @@ int64_t step_ctas(const DevSys& s, const LineGeom& g)
 
 /* ------------------------------------------------------------- run graph */
 
-template <int POT, int INTER>
+template <int POT, int INTER, bool TH = false>
 static void* line_kernel_t(int ppt)
 {
-    return ppt == 2 ? (void*)k_step_line<POT, INTER, 2> : (void*)k_step_line<POT, INTER, 1>;
+    return ppt == 2 ? (void*)k_step_line<POT, INTER, 2, STEP_SOFT, TH> : (void*)k_step_line<POT, INTER, 1, STEP_SOFT, TH>;
 }
 
 static void* step_kernel(const DevSys& s, const LineGeom& g)
 {
+    if (s.f_th) {
+        /* RandomNormalForcing systems: Cuspy with Laplace1d, Quartic1d or no interactions */
+        switch (s.inter) {
+            case INTER_LAPLACE1D: return line_kernel_t<POT_CUSPY, INTER_LAPLACE1D, true>(g.ppt);
+            case INTER_QUARTIC1D: return line_kernel_t<POT_CUSPY, INTER_QUARTIC1D, true>(g.ppt);
+            default: return line_kernel_t<POT_CUSPY, INTER_NONE, true>(g.ppt);
+        }
+    }
     if (s.inter == INTER_LONGRANGE1D) {
         return g.ppt == 2 ? (void*)k_lr_step<POT_CUSPY, 2> : (void*)k_lr_step<POT_CUSPY, 1>;
     }
@@ -1458,7 +1640,10 @@ cudaError_t launch_iteration(const DevSys& s, const LineGeom& g0, cudaStream_t s
     void* args2[] = {(void*)&s, (void*)&pass2};
     void* argsr[] = {(void*)&s};
     cudaError_t e = cudaSuccess;
-    if (s.inter == INTER_LONGRANGE1D) {
+    if (s.f_th) {
+        e = launch_thermal_draw(s, 1, 0, st);
+    }
+    if (e == cudaSuccess && s.inter == INTER_LONGRANGE1D) {
         e = cudaLaunchKernel((void*)k_lr_position, dim3((unsigned)((s.N + 255) / 256)), dim3(256), argsr, 0, st);
     }
     if (e == cudaSuccess) {
@@ -1522,7 +1707,18 @@ cudaError_t build_run_graph(DevSys& s, const LineGeom& g0, cudaGraphExec_t* exec
     void* args2[] = {(void*)&s, (void*)&pass2};
     void* argsr[] = {(void*)&s};
     cudaGraphNode_t nstep, nif;
-    if (s.inter == INTER_LONGRANGE1D) {
+    int th_from_ctl = 1;
+    int64_t th_inc = 0;
+    void* argst[] = {(void*)&s, (void*)&th_from_ctl, (void*)&th_inc};
+    if (s.f_th) {
+        /* updated_inc of the step: thermal draws before the step's forces */
+        cudaGraphNode_t ncount, ndraw;
+        dim3 gth((unsigned)thermal_tiles(s.N));
+        GR(add_kernel(&ncount, body, nullptr, 0, (void*)k_th_count, gth, dim3(256), argst));
+        GR(add_kernel(&ndraw, body, &ncount, 1, (void*)k_th_draw, gth, dim3(256), argst));
+        GR(add_kernel(&nstep, body, &ndraw, 1, fstep, grid, block, args1));
+    }
+    else if (s.inter == INTER_LONGRANGE1D) {
         /* all new positions before the all-pairs interaction */
         cudaGraphNode_t npos;
         GR(add_kernel(&npos, body, nullptr, 0, (void*)k_lr_position, dim3((unsigned)((s.N + 255) / 256)), dim3(256),

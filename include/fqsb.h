@@ -158,6 +158,26 @@ int fqsb_chunk_state_at(fqsb_system* h, const int64_t* index, uint64_t* state);
 int fqsb_chunk_restore(fqsb_system* h, const uint64_t* state, const double* value, const int64_t* index);
 
 /*
+ * RandomNormalForcing (thermal forcing): Line1d.System_Cuspy_Laplace_RandomForcing (Line1d.h:264-330,
+ * main.cpp:570-621), Line1d.System_Cuspy_Quartic_RandomForcing (main.cpp:623-676) and
+ * Particles.System_Cuspy_RandomForcing (main.cpp:335-384); the force itself is
+ * detail::RandomNormalForcing, detail.h:881-1000.  Every time step (inc++ first), each particle with
+ * inc >= next[p] redraws f_thermal[p] = mean + (stddev sqrt 2) erfinv(2 r - 1), r = u32 2^-32, from one
+ * pcg32 stream (seeded with `seed` on the default PCG stream), in particle order, and next[p] +=
+ * dinc[p]; f = ((((f_frame + f_potential) + f_interactions) + f_damping) + f_thermal).  Attach once,
+ * right after fqsb_create (the reference constructs it with the system): it draws at the current inc
+ * as the constructor's refresh does.  Cuspy potential with Laplace1d, Quartic1d or no interactions.
+ * fqsb_set_inc and fqsb_refresh draw as updated_inc does (detail.h:1241-1247, 1310-1315, 1369-1375).
+ */
+int fqsb_set_random_forcing(fqsb_system* h, double mean, double stddev, uint64_t seed, const int64_t* dinc_init,
+                            const int64_t* dinc);
+/* system.external members (main.cpp:253-269): the stream's state, f_thermal [N] and next [N]; any
+ * pointer may be NULL.  Setting f_thermal leaves f as it is until the next force update, as
+ * RandomNormalForcing::set_f_thermal does. */
+int fqsb_random_forcing_get(fqsb_system* h, uint64_t* state, double* f_thermal, int64_t* next);
+int fqsb_random_forcing_set(fqsb_system* h, const uint64_t* state, const double* f_thermal, const int64_t* next);
+
+/*
  * Device-resident variants for callers that keep data on the GPU (pointers
  * are device pointers of N doubles on the handle's device).
  */

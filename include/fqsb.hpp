@@ -10,6 +10,7 @@
 #define FQSB_HPP
 
 #include <array>
+#include <cstddef>
 #include <cstdint>
 #include <stdexcept>
 #include <string>
@@ -32,6 +33,61 @@ inline int distribution_id(const std::string& name)
     if (name == "normal") return FQSB_DIST_NORMAL;
     throw std::runtime_error("Unknown distribution: " + name);
 }
+
+/* system.external() of the RandomForcing systems (detail::RandomNormalForcing, detail.h:881-1000):
+ * the pcg32 state of the draws, the thermal forces and each particle's next draw increment. */
+class RandomNormalForcing {
+    fqsb_system* m_h = nullptr;
+    int64_t m_N = 0;
+
+    void check(int status) const
+    {
+        if (status != FQSB_OK) {
+            throw std::runtime_error(fqsb_last_error(m_h));
+        }
+    }
+
+public:
+    void bind(fqsb_system* h, int64_t N)
+    {
+        m_h = h;
+        m_N = N;
+    }
+    uint64_t state() const
+    {
+        uint64_t s = 0;
+        check(fqsb_random_forcing_get(m_h, &s, nullptr, nullptr));
+        return s;
+    }
+    void set_state(uint64_t s) { check(fqsb_random_forcing_set(m_h, &s, nullptr, nullptr)); }
+    std::vector<double> f_thermal() const
+    {
+        std::vector<double> out((size_t)m_N);
+        check(fqsb_random_forcing_get(m_h, nullptr, out.data(), nullptr));
+        return out;
+    }
+    void set_f_thermal(const std::vector<double>& f)
+    {
+        if ((int64_t)f.size() != m_N) {
+            throw std::runtime_error("assertion failed (xt::has_shape(f_thermal, m_f_thermal.shape()))");
+        }
+        check(fqsb_random_forcing_set(m_h, nullptr, f.data(), nullptr));
+    }
+    std::vector<ptrdiff_t> next() const
+    {
+        std::vector<int64_t> out((size_t)m_N);
+        check(fqsb_random_forcing_get(m_h, nullptr, nullptr, out.data()));
+        return std::vector<ptrdiff_t>(out.begin(), out.end());
+    }
+    void set_next(const std::vector<ptrdiff_t>& n)
+    {
+        if ((int64_t)n.size() != m_N) {
+            throw std::runtime_error("assertion failed (xt::has_shape(next, m_next.shape()))");
+        }
+        std::vector<int64_t> v(n.begin(), n.end());
+        check(fqsb_random_forcing_set(m_h, nullptr, nullptr, v.data()));
+    }
+};
 
 /* Generic system (detail::System, detail.h:1046-2051) resident on one GPU. */
 class System {
@@ -89,6 +145,20 @@ protected:
         m_eta = eta;
         m_m = m;
         m_k_frame = k_frame;
+    }
+
+    RandomNormalForcing m_ext;
+
+    /* RandomNormalForcing constructor (detail.h:903-919) + the system constructor's refresh */
+    void attach_random_forcing(double mean, double stddev, uint64_t seed_forcing,
+                               const std::vector<ptrdiff_t>& dinc_init, const std::vector<ptrdiff_t>& dinc)
+    {
+        if ((int64_t)dinc_init.size() != m_N || (int64_t)dinc.size() != m_N) {
+            throw std::runtime_error("dinc_init and dinc must have one entry per particle");
+        }
+        std::vector<int64_t> a(dinc_init.begin(), dinc_init.end()), b(dinc.begin(), dinc.end());
+        check(fqsb_set_random_forcing(m_h, mean, stddev, seed_forcing, a.data(), b.data()));
+        m_ext.bind(m_h, m_N);
     }
 
     std::vector<double> field(int which) const
@@ -286,6 +356,40 @@ public:
     }
 };
 
+/* Line1d.h:264-330: Cuspy + Laplace1d with RandomNormalForcing */
+class System_Cuspy_Laplace_RandomForcing : public System {
+public:
+    System_Cuspy_Laplace_RandomForcing(double m, double eta, double mu, double k_interactions, double k_frame,
+                                       double dt, double mean, double stddev, uint64_t seed_forcing,
+                                       const std::vector<ptrdiff_t>& dinc_init, const std::vector<ptrdiff_t>& dinc,
+                                       const std::array<size_t, 1>& shape, uint64_t seed,
+                                       const std::string& distribution, const std::vector<double>& parameters,
+                                       double offset = -100.0, size_t nchunk = 5000)
+    {
+        init(FQSB_CUSPY, FQSB_LAPLACE1D, 1, (int64_t)shape[0], m, eta, mu, 0.0, k_interactions, k_frame, dt, seed,
+             distribution, parameters, offset, nchunk);
+        attach_random_forcing(mean, stddev, seed_forcing, dinc_init, dinc);
+    }
+    RandomNormalForcing* external() { return &m_ext; }
+};
+
+/* Line1d.h:486-556: Cuspy + Quartic1d with RandomNormalForcing */
+class System_Cuspy_Quartic_RandomForcing : public System {
+public:
+    System_Cuspy_Quartic_RandomForcing(double m, double eta, double mu, double a1, double a2, double k_frame,
+                                       double dt, double mean, double stddev, uint64_t seed_forcing,
+                                       const std::vector<ptrdiff_t>& dinc_init, const std::vector<ptrdiff_t>& dinc,
+                                       const std::array<size_t, 1>& shape, uint64_t seed,
+                                       const std::string& distribution, const std::vector<double>& parameters,
+                                       double offset = -100.0, size_t nchunk = 5000)
+    {
+        init(FQSB_CUSPY, FQSB_QUARTIC1D, 1, (int64_t)shape[0], m, eta, mu, 0.0, 0.0, k_frame, dt, seed, distribution,
+             parameters, offset, nchunk, a1, a2);
+        attach_random_forcing(mean, stddev, seed_forcing, dinc_init, dinc);
+    }
+    RandomNormalForcing* external() { return &m_ext; }
+};
+
 /* Line1d.h:428-481 */
 class System_Cuspy_Quartic : public System {
 public:
@@ -365,6 +469,22 @@ public:
         init(FQSB_CUSPY, FQSB_INTERACTIONS_NONE, 1, (int64_t)shape[0], m, eta, mu, 0.0, 0.0, k_frame, dt, seed,
              distribution, parameters, offset, nchunk);
     }
+};
+
+/* Particles.h:161-227: independent Cuspy particles with RandomNormalForcing */
+class System_Cuspy_RandomForcing : public System {
+public:
+    System_Cuspy_RandomForcing(double m, double eta, double mu, double k_frame, double dt, double mean, double stddev,
+                               uint64_t seed_forcing, const std::vector<ptrdiff_t>& dinc_init,
+                               const std::vector<ptrdiff_t>& dinc, const std::array<size_t, 1>& shape, uint64_t seed,
+                               const std::string& distribution, const std::vector<double>& parameters,
+                               double offset = -100.0, size_t nchunk = 5000)
+    {
+        init(FQSB_CUSPY, FQSB_INTERACTIONS_NONE, 1, (int64_t)shape[0], m, eta, mu, 0.0, 0.0, k_frame, dt, seed,
+             distribution, parameters, offset, nchunk);
+        attach_random_forcing(mean, stddev, seed_forcing, dinc_init, dinc);
+    }
+    RandomNormalForcing* external() { return &m_ext; }
 };
 
 class System_SemiSmooth : public System {

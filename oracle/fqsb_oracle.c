@@ -868,6 +868,41 @@ int oq_set_thermal(oq_system* s, double mean, double stddev, uint64_t state, uin
     return OQ_OK;
 }
 
+int oq_thermal_get(oq_system* s, uint64_t* state, double* f_thermal, int64_t* next)
+{
+    if (!s->thermal) {
+        return fail(s, OQ_ERR_INVALID, "no RandomNormalForcing attached");
+    }
+    if (state) {
+        *state = s->th_state;
+    }
+    if (f_thermal) {
+        memcpy(f_thermal, s->f_th, sizeof(double) * (size_t)s->N);
+    }
+    if (next) {
+        memcpy(next, s->th_next, sizeof(int64_t) * (size_t)s->N);
+    }
+    return OQ_OK;
+}
+
+/* set_state (prrng restore: the state, the stream kept), set_f_thermal, set_next: detail.h:956-995 */
+int oq_thermal_set(oq_system* s, const uint64_t* state, const double* f_thermal, const int64_t* next)
+{
+    if (!s->thermal) {
+        return fail(s, OQ_ERR_INVALID, "no RandomNormalForcing attached");
+    }
+    if (state) {
+        s->th_state = *state;
+    }
+    if (f_thermal) {
+        memcpy(s->f_th, f_thermal, sizeof(double) * (size_t)s->N);
+    }
+    if (next) {
+        memcpy(s->th_next, next, sizeof(int64_t) * (size_t)s->N);
+    }
+    return OQ_OK;
+}
+
 int oq_get_thermal(oq_system* s, double* f_thermal)
 {
     if (!s->thermal) {

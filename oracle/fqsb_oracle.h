@@ -115,6 +115,10 @@ int oq_set_interaction_parameters(oq_system* s, double a, double b);
 int oq_set_thermal(oq_system* s, double mean, double stddev, uint64_t state, uint64_t inc, const int64_t* next,
                    const int64_t* dinc, int mode);
 int oq_get_thermal(oq_system* s, double* f_thermal);
+/* RandomNormalForcing members state / f_thermal / next (detail.h:947-995); NULL pointers are skipped.
+ * Setting f_thermal does not recompute f (set_f_thermal). */
+int oq_thermal_get(oq_system* s, uint64_t* state, double* f_thermal, int64_t* next);
+int oq_thermal_set(oq_system* s, const uint64_t* state, const double* f_thermal, const int64_t* next);
 int oq_minimise(oq_system* s, double tol, uint64_t niter_tol, uint64_t max_iter, int time_activity,
                 int max_iter_is_error, uint64_t* ret);
 int oq_minimise_truncate(oq_system* s, const int64_t* i_n, uint64_t A_truncate, uint64_t S_truncate,

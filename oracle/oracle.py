@@ -111,6 +111,8 @@ def lib():
         L.oq_set_interaction_parameters.argtypes = [P, d, d]
         L.oq_set_thermal.argtypes = [P, d, d, u64, u64, P, P, i32]
         L.oq_get_thermal.argtypes = [P, pd]
+        L.oq_thermal_get.argtypes = [P, P, P, P]
+        L.oq_thermal_set.argtypes = [P, P, P, P]
         L.oq_minimise_truncate.argtypes = [P, P, u64, u64, d, u64, u64, i32, i32, ctypes.POINTER(u64)]
         L.oq_max_uniform_displacement.argtypes = [P, i32, pd]
         L.oq_event_driven_step.argtypes = [P, d, i32, i32, pd]
@@ -339,6 +341,33 @@ class System:
         self._check(lib().oq_get_thermal(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
         return out.reshape(self.shape)
 
+    @f_thermal.setter
+    def f_thermal(self, value):
+        a = np.ascontiguousarray(np.broadcast_to(value, self.shape), dtype=np.float64).ravel()
+        self._check(lib().oq_thermal_set(self._h, None, a.ctypes.data, None))
+
+    @property
+    def thermal_state(self):
+        out = ctypes.c_uint64()
+        self._check(lib().oq_thermal_get(self._h, ctypes.addressof(out), None, None))
+        return out.value
+
+    @thermal_state.setter
+    def thermal_state(self, value):
+        st = ctypes.c_uint64(int(value))
+        self._check(lib().oq_thermal_set(self._h, ctypes.addressof(st), None, None))
+
+    @property
+    def thermal_next(self):
+        out = np.empty(self.size, np.int64)
+        self._check(lib().oq_thermal_get(self._h, None, None, out.ctypes.data))
+        return out.reshape(self.shape)
+
+    @thermal_next.setter
+    def thermal_next(self, value):
+        a = np.ascontiguousarray(np.broadcast_to(value, self.shape), dtype=np.int64).ravel()
+        self._check(lib().oq_thermal_set(self._h, None, None, a.ctypes.data))
+
     def minimise_nopassing(self, tol=1e-5, niter_tol=10, max_iter=int(1e9), max_iter_is_error=True):
         r = ctypes.c_uint64()
         self._check(lib().oq_minimise_nopassing(self._h, tol, niter_tol, int(max_iter), int(max_iter_is_error),
@@ -451,6 +480,18 @@ def pcg32_randint(seed, n, high, initseq=PCG32_DEFAULT_STREAM):
     return out
 
 
+def attach_random_forcing(s, mean, stddev, seed_forcing, dinc_init, dinc):
+    """RandomNormalForcing (detail.h:881-1000) on an oracle system, drawn at its current inc as the
+    RandomForcing constructors' refresh does."""
+    n = s.size
+    s._th_next = np.ascontiguousarray(np.broadcast_to(dinc_init, (n,)), dtype=np.int64)
+    s._th_dinc = np.ascontiguousarray(np.broadcast_to(dinc, (n,)), dtype=np.int64)
+    state, inc = pcg32_seed(int(seed_forcing))
+    s._check(lib().oq_set_thermal(s._h, float(mean), float(stddev), state, inc, s._th_next.ctypes.data,
+                                  s._th_dinc.ctypes.data, 0))
+    return s
+
+
 def line1d_random_forcing(m, eta, mu, k_interactions, k_frame, dt, mean, stddev, seed_forcing, dinc_init, dinc,
                           shape, seed, distribution, parameters, offset=-100.0, nchunk=5000, **kw):
     """System_Cuspy_Laplace_RandomForcing (Line1d.h:264-330, RandomNormalForcing detail.h:881-1000):
@@ -460,13 +501,7 @@ def line1d_random_forcing(m, eta, mu, k_interactions, k_frame, dt, mean, stddev,
     s = System(CUSPY, LAPLACE1D, shape=shape, m=m, eta=eta, mu=mu, k_interactions=k_interactions, k_frame=k_frame,
                dt=dt, seed=seed, distribution=distribution, parameters=parameters, offset=offset, nchunk=nchunk,
                **kw)
-    n = s.size
-    s._th_next = np.ascontiguousarray(np.broadcast_to(dinc_init, (n,)), dtype=np.int64)
-    s._th_dinc = np.ascontiguousarray(np.broadcast_to(dinc, (n,)), dtype=np.int64)
-    state, inc = pcg32_seed(int(seed_forcing))
-    s._check(lib().oq_set_thermal(s._h, float(mean), float(stddev), state, inc, s._th_next.ctypes.data,
-                                  s._th_dinc.ctypes.data, 0))
-    return s
+    return attach_random_forcing(s, mean, stddev, seed_forcing, dinc_init, dinc)
 
 
 def line2d(**kw):

@@ -65,6 +65,16 @@ def test_cpp_header_compiles(tmp_path):
 #include "fqsb.hpp"
 using namespace FrictionQPotSpringBlock_gb300;
 template <class T> void touch(T* s) { if (s) { s->minimise(); s->u(); } }
+template <class T> void touch_th(T* s)
+{
+    if (s) {
+        s->flowSteps(10, 0.1);
+        auto* e = s->external();
+        e->set_state(e->state());
+        e->set_next(e->next());
+        e->set_f_thermal(e->f_thermal());
+    }
+}
 int main()
 {
     touch<Line1d::System_Cuspy_Laplace>(nullptr);
@@ -77,6 +87,9 @@ int main()
     touch<Line2d::System_Cuspy_Laplace>(nullptr);
     touch<Line2d::System_Cuspy_QuarticGradient>(nullptr);
     touch<Particles::System_Cuspy>(nullptr);
+    touch_th<Line1d::System_Cuspy_Laplace_RandomForcing>(nullptr);
+    touch_th<Line1d::System_Cuspy_Quartic_RandomForcing>(nullptr);
+    touch_th<Particles::System_Cuspy_RandomForcing>(nullptr);
     return 0;
 }
 """)
