@@ -5,12 +5,13 @@
  * helpers, chunk restore).
  *
  * Forces are not stored per step: f_potential, f_interactions, f_frame, f_damping and f are
- * pure functions of (u, v, u_frame, current well) after every reference operation that calls
- * updated_u / updated_v, so getters recompute them from the state.  The one exception is
- * System::trigger (detail.h:1972-1977), which returns before updated_u and leaves the forces
- * stale; the handle then materialises the force arrays and updates them exactly as the
- * reference does (set_u_frame recomputes f_frame and f, set_v / quench recompute f_damping
- * and f) until the next operation that calls updated_u.
+ * pure functions of (u, v, u_frame, current well, and f_thermal for RandomForcing systems) after
+ * every reference operation that calls updated_u / updated_v, so getters recompute them from the
+ * state.  The exceptions are System::trigger (detail.h:1972-1977), which returns before updated_u
+ * and leaves the forces stale, and RandomNormalForcing::set_f_thermal (detail.h:972-976), which
+ * leaves f as it was; the handle then materialises the force arrays and updates them exactly as
+ * the reference does (set_u_frame recomputes f_frame and f, set_v / quench / set_inc recompute
+ * f_damping and f) until the next operation that calls updated_u.
  */
 #include <algorithm>
 #include <cstdlib>
