@@ -239,6 +239,58 @@ def bench_small(fqsb, cycles=20, cpu_cycles=3):
     return out
 
 
+def bench_next_rows(fqsb, n=2 ** 22, side=2048, n_lr=16384, n_np=2 ** 17, steps=200):
+    """The further interaction types and the no-passing minimiser, each on its own system (Cuspy,
+    Weibull(2,1)+1e-5 seed 2, 200-position chunk, m = 1, eta = 0.1, mu = 1, dt = 0.1, k_frame = 1/N,
+    u ~ N(0, 0.1^2)), timed with the handle's synchronous calls after 20 warm-up steps:
+    flowSteps(steps, 1e-3) for Line1d Quartic (a1 = a2 = 1) and QuarticGradient (k2 = k4 = 1) at
+    N = 2^22 and Line2d QuarticGradient at 2048 x 2048; flowSteps(steps // 5) for Line1d LongRange
+    (alpha = 1, k = 1, all pairs) at N = 16384; the no-passing minimiser (Line1d Nopassing, N = 2^17)
+    after a +0.5 frame jump, bounded at 5000 sweeps.  A failure is recorded, not raised."""
+    par = dict(eta=0.1, mu=1.0, dt=0.1, seed=2, distribution="weibull", parameters=[2.0, 1.0, 1e-5], offset=-100.0,
+               nchunk=200)
+    out = {}
+
+    def flow(name, make, size, nsteps, extra=None):
+        try:
+            s = make()
+            s.u = np.random.default_rng(2).normal(0.0, 0.1, size).reshape(s.shape)
+            s.flowSteps(20, V_FRAME)
+            t0 = time.perf_counter()
+            s.flowSteps(nsteps, V_FRAME)
+            dt = time.perf_counter() - t0
+            r = {"particles": size, "steps": nsteps, "seconds": dt, "particle_steps_per_s": size * nsteps / dt}
+            if extra:
+                r.update(extra(size, nsteps, dt))
+            out[name] = r
+            del s
+        except Exception as e:  # noqa: BLE001 -- the bench line must still be printed
+            out[name] = {"error": f"{type(e).__name__}: {e}"}
+
+    flow("Line1d_Cuspy_Quartic", lambda: fqsb.Line1d.System_Cuspy_Quartic(
+        m=1.0, a1=1.0, a2=1.0, k_frame=1.0 / n, shape=[n], **par), n, steps)
+    flow("Line1d_Cuspy_QuarticGradient", lambda: fqsb.Line1d.System_Cuspy_QuarticGradient(
+        m=1.0, k2=1.0, k4=1.0, k_frame=1.0 / n, shape=[n], **par), n, steps)
+    flow("Line2d_Cuspy_QuarticGradient", lambda: fqsb.Line2d.System_Cuspy_QuarticGradient(
+        m=1.0, k2=1.0, k4=1.0, k_frame=1.0 / side ** 2, shape=[side, side], **par), side * side, steps)
+    flow("Line1d_Cuspy_LongRange", lambda: fqsb.Line1d.System_Cuspy_LongRange(
+        m=1.0, k_interactions=1.0, alpha=1.0, k_frame=1.0 / n_lr, shape=[n_lr], **par), n_lr, steps // 5,
+        extra=lambda size, k, dt: {"pair_terms_per_s": size * (size - 1) * k / dt})
+    try:
+        s = fqsb.Line1d.System_Cuspy_Laplace_Nopassing(mu=1.0, k_interactions=1.0, k_frame=1.0 / n_np, shape=[n_np],
+                                                       **{k: v for k, v in par.items() if k not in ("eta", "dt", "mu")})
+        s.u_frame = 0.5
+        t0 = time.perf_counter()
+        ret = s.minimise(max_iter=5000, max_iter_is_error=False)
+        dt = time.perf_counter() - t0
+        out["Line1d_Cuspy_Laplace_Nopassing"] = {"particles": n_np, "seconds": dt, "converged": ret == 0,
+                                                 "max_iter": 5000}
+        del s
+    except Exception as e:  # noqa: BLE001
+        out["Line1d_Cuspy_Laplace_Nopassing"] = {"error": f"{type(e).__name__}: {e}"}
+    return out
+
+
 def cpu_baseline_sample(n_sample=2 ** 16, steps=3000, repeats=1):
     """Time the CPU oracle (loop-per-statement restatement of the reference, libm, sequential sums)
     on a bounded sample of the same workload: the first n_sample particles' parameters on a ring of
@@ -429,6 +481,7 @@ def main():
         forms["batched"] = bench_batched(fqsb)
         forms["adjoint"] = bench_adjoint(fqsb)
         forms["small_system"] = bench_small(fqsb)
+        forms["next_rows"] = bench_next_rows(fqsb)
 
     if rank != 0:
         return
