@@ -421,82 +421,75 @@ FQ_HD double fq_cos(double x)
 }
 
 /* ---------------------------------------------------------------- erf / erfc / erfinv
- * For the normal quantile of thermal forcing, mean + stddev sqrt(2) erfinv(2 r - 1).  erf by its
- * Maclaurin series and erfc by its Laplace continued fraction, both in double-double; erfinv by Newton
- * steps on those from Winitzki's closed-form approximation ("A handy approximation for the error
- * function and its inverse", 2008).  Host and device run the same code, so they agree bit for bit.
+ * For the normal quantile of thermal forcing, mean + stddev sqrt(2) erfinv(2 r - 1).
+ *
+ * erf near a grid point.  With x_i = i/64 and G_i = (2/sqrt(pi)) exp(-x_i^2),
+ *     (2/sqrt(pi)) exp(-(x_i + h)^2) = G_i sum_k p_k h^k,   p_0 = 1, p_1 = -2 x_i,
+ *     (k + 1) p_{k+1} = -2 x_i p_k - 2 p_{k-1}               (Taylor series of exp(-2 x_i h - h^2)),
+ * so erf(x_i + h) = erf(x_i) + G_i S(h) and erfc(x_i + h) = erfc(x_i) - G_i S(h) with
+ * S(h) = sum_k p_k h^(k+1) / (k+1).  erf(x_i), erfc(x_i) and G_i come as double-doubles from a table
+ * (fq_erf_table.h, 60-digit mpmath); with |h| <= 1/128, 16 terms leave a truncation error below
+ * 1e-29 relative to G_i, so the double-double sum resolves erfc(x) to ~1e-27 relative up to x = 6.
+ *
+ * erfinv(y): bracket |y| (or 1 - |y| > 1/2, which is exact, against erfc) in the table, interpolate
+ * linearly (error <= 4e-4), then three Halley steps x -= d / (1 + x d), d = residual / derivative: the
+ * first with a double residual (error ~1e-9 after it), the last two with the double-double residual.
+ * The last step's correction is below an ulp and is computed to ~16 digits, so the result is the
+ * correctly rounded erfinv except within ~1e-16 ulp of a rounding midpoint.  Host and device run the
+ * same code (the table is duplicated into device memory), so they agree bit for bit.
  */
-#define FQ_2_SQRTPI_HI 0x1.20dd750429b6dp+0
-#define FQ_2_SQRTPI_LO 0x1.1ae3a914fed80p-56
-#define FQ_1_SQRTPI_HI 0x1.20dd750429b6dp-1
-#define FQ_1_SQRTPI_LO 0x1.1ae3a914fed80p-57
+#include "fq_erf_table.h"
 
-/* x / d for a double-double x and a double d. */
-FQ_HD fq_dd fq_dd_div_d(fq_dd x, double d)
+#define FQ_ERF_K 16
+
+#if defined(__CUDACC__)
+__device__ static const double fq_erf_tab_dev[FQ_ERF_N][6] = FQ_ERF_TABLE_INIT;
+__device__ static const double fq_inv_tab_dev[FQ_INV_N][2] = FQ_INV_TABLE_INIT;
+#endif
+static const double fq_erf_tab_host[FQ_ERF_N][6] = FQ_ERF_TABLE_INIT;
+static const double fq_inv_tab_host[FQ_INV_N][2] = FQ_INV_TABLE_INIT;
+
+/* row i of the erf table: erf hi, lo, erfc hi, lo, G hi, lo */
+FQ_HD const double* fq_erf_row(int i)
 {
-    double q1 = FQ_DIV(x.hi, d);
-    fq_dd p = fq_two_prod(q1, d);
-    double r = FQ_ADD(FQ_SUB(FQ_SUB(x.hi, p.hi), p.lo), x.lo);
-    return fq_fast_two_sum(q1, FQ_DIV(r, d));
+#if defined(__CUDA_ARCH__)
+    return fq_erf_tab_dev[i];
+#else
+    return fq_erf_tab_host[i];
+#endif
 }
 
-/* x / y for double-doubles (one correction step; y > 0 here). */
-FQ_HD fq_dd fq_dd_div(fq_dd x, fq_dd y)
+/* 1/k as a double-double, 1 <= k < FQ_INV_N */
+FQ_HD fq_dd fq_inv_k(int k)
 {
-    double q1 = FQ_DIV(x.hi, y.hi);
-    fq_dd r = fq_dd_add(x, fq_dd_neg(fq_dd_mul_d(y, q1)));
-    double q2 = FQ_DIV(r.hi, y.hi);
-    return fq_fast_two_sum(q1, q2);
+#if defined(__CUDA_ARCH__)
+    return fq_dd_make(fq_inv_tab_dev[k][0], fq_inv_tab_dev[k][1]);
+#else
+    return fq_dd_make(fq_inv_tab_host[k][0], fq_inv_tab_host[k][1]);
+#endif
 }
 
-/* exp of a double-double argument in [-745, 0], as a double-double (no rounding to double). */
-FQ_HD fq_dd fq_exp_dd_full(fq_dd P)
+/* Coefficients of grid point i: q_k = p_k / (k+1) (double-double) and p_k (double). */
+FQ_HD void fq_erf_coeffs(int i, fq_dd* q, double* p)
 {
-    double kf = FQ_MUL(P.hi, FQ_INV_LN2);
-    int n = (int)(kf >= 0.0 ? FQ_ADD(kf, 0.5) : FQ_SUB(kf, 0.5));
-    fq_dd r = fq_dd_add(P, fq_dd_neg(fq_dd_mul_d(fq_dd_make(FQ_LN2_HI, FQ_LN2_LO), (double)n)));
-    double ch, cl;
-    fq_inv_factorial(20, &ch, &cl);
-    fq_dd p = fq_dd_make(ch, cl);
-    for (int k = 19; k >= 0; --k) {
-        fq_inv_factorial(k, &ch, &cl);
-        p = fq_dd_add(fq_dd_mul(p, r), fq_dd_make(ch, cl));
+    const double m2x = FQ_MUL(-(double)i, 0x1p-5); /* -2 x_i, exact */
+    fq_dd pm = fq_dd_make(0.0, 0.0);
+    fq_dd pk = fq_dd_make(1.0, 0.0);
+    for (int k = 0; k < FQ_ERF_K; ++k) {
+        const fq_dd inv = fq_inv_k(k + 1);
+        p[k] = pk.hi;
+        q[k] = fq_dd_mul(pk, inv);
+        fq_dd t = fq_dd_add(fq_dd_mul_d(pk, m2x), fq_dd_make(FQ_MUL(-2.0, pm.hi), FQ_MUL(-2.0, pm.lo)));
+        pm = pk;
+        pk = fq_dd_mul(t, inv);
     }
-    const double sc = fq_pow2i(n < -1022 ? -1022 : n); /* the callers stay far above the subnormals */
-    return fq_dd_make(FQ_MUL(p.hi, sc), FQ_MUL(p.lo, sc));
 }
 
-/* erf(x), 0 <= x <= 2.5, double-double: (2/sqrt(pi)) sum_n (-1)^n x^(2n+1) / (n! (2n+1)). */
-FQ_HD fq_dd fq_erf_series(double x)
+/* nearest grid point of x >= 0 */
+FQ_HD int fq_erf_cell(double x)
 {
-    const fq_dd x2 = fq_two_prod(x, x);
-    fq_dd t = fq_dd_make(x, 0.0); /* x^(2n+1) / n! */
-    fq_dd sum = t;
-    for (int n = 1; n < 120; ++n) {
-        t = fq_dd_div_d(fq_dd_mul(t, x2), (double)n);
-        fq_dd term = fq_dd_div_d(t, (double)(2 * n + 1));
-        sum = fq_dd_add(sum, (n & 1) ? fq_dd_neg(term) : term);
-        if (FQ_MUL(1e34, (term.hi < 0.0 ? -term.hi : term.hi)) < (sum.hi < 0.0 ? -sum.hi : sum.hi)) {
-            break;
-        }
-    }
-    return fq_dd_mul(sum, fq_dd_make(FQ_2_SQRTPI_HI, FQ_2_SQRTPI_LO));
-}
-
-/* erfc(x), x >= 0, double-double: 1 - erf below 2.5, the continued fraction
- * erfc(x) = exp(-x^2) / (sqrt(pi) (x + (1/2) / (x + (2/2) / (x + (3/2) / ...)))) above (80 terms,
- * evaluated from the tail). */
-FQ_HD fq_dd fq_erfc_dd(double x)
-{
-    if (x < 2.5) {
-        return fq_dd_add(fq_dd_make(1.0, 0.0), fq_dd_neg(fq_erf_series(x)));
-    }
-    fq_dd t = fq_dd_make(x, 0.0);
-    for (int k = 80; k >= 1; --k) {
-        t = fq_dd_add(fq_dd_make(x, 0.0), fq_dd_div(fq_dd_make(FQ_MUL(0.5, (double)k), 0.0), t));
-    }
-    fq_dd e = fq_exp_dd_full(fq_dd_neg(fq_two_prod(x, x)));
-    return fq_dd_div(fq_dd_mul(e, fq_dd_make(FQ_1_SQRTPI_HI, FQ_1_SQRTPI_LO)), t);
+    int i = (int)FQ_ADD(FQ_MUL(x, 64.0), 0.5);
+    return i < FQ_ERF_N - 1 ? i : FQ_ERF_N - 1;
 }
 
 /* erfinv(y), -1 <= y <= 1. */
@@ -515,26 +508,73 @@ FQ_HD double fq_erfinv(double y)
     if (a == 0.0) {
         return y;
     }
-    /* Winitzki: x^2 = sqrt(b^2 - ln(1 - a^2) / c) - b, b = 2 / (pi c) + ln(1 - a^2) / 2, c = 0.147 */
-    const double c = 0.147;
-    const double L = fq_log(FQ_MUL(FQ_SUB(1.0, a), FQ_ADD(1.0, a)));
-    const double b = FQ_ADD(FQ_DIV(0x1.45f306dc9c883p-1, c), FQ_MUL(0.5, L));
-    double x = FQ_SQRT(FQ_SUB(FQ_SQRT(FQ_SUB(FQ_MUL(b, b), FQ_DIV(L, c))), b));
+    if (a < 0x1p-500) {
+        /* erfinv(a) = a sqrt(pi)/2 (1 + pi a^2 / 12 + ...): the correction is below 2^-1000 */
+        const double s = FQ_MUL(a, 0x1p+600);
+        fq_dd pr = fq_two_prod(s, 0x1.c5bf891b4ef6bp-1);
+        double x = FQ_ADD(pr.hi, FQ_ADD(pr.lo, FQ_MUL(s, -0x1.618f13eb7ca89p-55)));
+        x = FQ_MUL(x, 0x1p-600);
+        return y < 0.0 ? -x : x;
+    }
+    const int tail = a > 0.5;
     const double q = FQ_SUB(1.0, a); /* exact for a >= 1/2 */
-    for (int it = 0; it < 6; ++it) {
-        /* Newton on erf(x) = a (small a) or erfc(x) = 1 - a (relative accuracy in the tail) */
-        const double d = FQ_MUL(FQ_2_SQRTPI_HI, fq_exp(-FQ_MUL(x, x)));
-        double r;
-        if (a <= 0.5) {
-            fq_dd e = fq_erf_series(x);
-            r = FQ_ADD(FQ_SUB(e.hi, a), e.lo);
-            x = FQ_SUB(x, FQ_DIV(r, d));
+    const double target = tail ? q : a;
+    /* bracket: the last grid point with erf(x_i) <= a (erfc(x_i) >= q in the tail) */
+    int lo = 0, hi = FQ_ERF_N - 1;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        const double v = fq_erf_row(mid)[tail ? 2 : 0];
+        if (tail ? v >= q : v <= a) {
+            lo = mid;
         }
         else {
-            fq_dd e = fq_erfc_dd(x);
-            r = FQ_ADD(FQ_SUB(e.hi, q), e.lo);
-            x = FQ_ADD(x, FQ_DIV(r, d));
+            hi = mid;
         }
+    }
+    const double f0 = fq_erf_row(lo)[tail ? 2 : 0];
+    const double f1 = fq_erf_row(lo + 1)[tail ? 2 : 0];
+    double t = FQ_DIV(FQ_SUB(target, f0), FQ_SUB(f1, f0));
+    t = t < 0.0 ? 0.0 : (t > 1.0 ? 1.0 : t);
+    double x = FQ_MUL(FQ_ADD((double)lo, t), 0x1p-6);
+
+    fq_dd qk[FQ_ERF_K];
+    double pk[FQ_ERF_K];
+    int cell = fq_erf_cell(x);
+    fq_erf_coeffs(cell, qk, pk);
+    for (int it = 0; it < 3; ++it) {
+        const int c = fq_erf_cell(x);
+        if (c != cell) {
+            cell = c;
+            fq_erf_coeffs(cell, qk, pk);
+        }
+        const double* row = fq_erf_row(cell);
+        const double h = FQ_SUB(x, FQ_MUL((double)cell, 0x1p-6)); /* exact */
+        double r;
+        if (it == 0) {
+            double s = qk[FQ_ERF_K - 1].hi;
+            for (int k = FQ_ERF_K - 2; k >= 0; --k) {
+                s = FQ_ADD(FQ_MUL(s, h), qk[k].hi);
+            }
+            const double gs = FQ_MUL(row[4], FQ_MUL(s, h));
+            r = tail ? FQ_SUB(FQ_SUB(row[2], gs), q) : FQ_SUB(FQ_ADD(row[0], gs), a);
+        }
+        else {
+            fq_dd s = qk[FQ_ERF_K - 1];
+            for (int k = FQ_ERF_K - 2; k >= 0; --k) {
+                s = fq_dd_add(fq_dd_mul_d(s, h), qk[k]);
+            }
+            const fq_dd gs = fq_dd_mul(fq_dd_make(row[4], row[5]), fq_dd_mul_d(s, h));
+            const fq_dd v = tail ? fq_dd_add(fq_dd_make(row[2], row[3]), fq_dd_neg(gs))
+                                 : fq_dd_add(fq_dd_make(row[0], row[1]), gs);
+            r = FQ_ADD(FQ_SUB(v.hi, target), v.lo);
+        }
+        double g = pk[FQ_ERF_K - 1];
+        for (int k = FQ_ERF_K - 2; k >= 0; --k) {
+            g = FQ_ADD(FQ_MUL(g, h), pk[k]);
+        }
+        const double deriv = FQ_MUL(row[4], g);
+        const double d = tail ? FQ_DIV(-r, deriv) : FQ_DIV(r, deriv);
+        x = FQ_SUB(x, FQ_DIV(d, FQ_ADD(1.0, FQ_MUL(x, d))));
     }
     return y < 0.0 ? -x : x;
 }
