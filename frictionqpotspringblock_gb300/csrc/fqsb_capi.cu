@@ -766,7 +766,7 @@ static void free_all(fqsb_system* h)
     void* ptrs[] = {d.data, d.start, d.cidx, d.gidx, d.wc, d.acc_end, d.anc_kind, d.anc_k, d.anc_state, d.anc_val,
                     d.u[0], d.u[1], d.v[0], d.v[1], d.a[0], d.a[1], d.ctl, d.ring, d.partials, d.i_n, d.sq2,
                     d.cta_pending, d.regen_list, (void*)d.lr_pref, d.f_th, d.th_next, (void*)d.th_dinc, d.th_cnt,
-                    d.th,
+                    d.th_list, d.th,
                     (void*)d.offp, h->scratch, h->red_partials, h->red_out, h->mkey, h->mflag, h->fs[0], h->fs[1],
                     h->fs[2], h->fs[3], h->fs[4], h->adj_sched, h->adj_ckpt, h->adj_ffsum, h->adj_final};
     for (void* p : ptrs) {
@@ -1437,6 +1437,7 @@ extern "C" int fqsb_set_random_forcing(fqsb_system* h, double mean, double stdde
     const int64_t G = thermal_tiles(N);
     double* f_th = nullptr;
     int64_t *next = nullptr, *di = nullptr, *cnt = nullptr;
+    int32_t* list = nullptr;
     Thermal* th = nullptr;
     cudaError_t e = cudaMalloc(&f_th, sizeof(double) * (size_t)padded(N));
     if (e == cudaSuccess) {
@@ -1449,6 +1450,9 @@ extern "C" int fqsb_set_random_forcing(fqsb_system* h, double mean, double stdde
         e = cudaMalloc(&cnt, sizeof(int64_t) * (size_t)G);
     }
     if (e == cudaSuccess) {
+        e = cudaMalloc(&list, sizeof(int32_t) * (size_t)N);
+    }
+    if (e == cudaSuccess) {
         e = cudaMalloc(&th, sizeof(Thermal));
     }
     /* prrng pcg32(seed): the PCG seeding procedure on the default stream */
@@ -1459,6 +1463,7 @@ extern "C" int fqsb_set_random_forcing(fqsb_system* h, double mean, double stdde
     t0.state += seed;
     t0.state = t0.state * PCG_MULT + t0.inc;
     t0.base = t0.state;
+    t0.total = 0;
     t0.ticket = 0u;
     t0.pad = 0u;
     if (e == cudaSuccess) {
@@ -1477,7 +1482,7 @@ extern "C" int fqsb_set_random_forcing(fqsb_system* h, double mean, double stdde
         e = cudaStreamSynchronize(h->stream);
     }
     if (e != cudaSuccess) {
-        for (void* q : {(void*)f_th, (void*)next, (void*)di, (void*)cnt, (void*)th}) {
+        for (void* q : {(void*)f_th, (void*)next, (void*)di, (void*)cnt, (void*)list, (void*)th}) {
             if (q) {
                 cudaFree(q);
             }
@@ -1488,6 +1493,7 @@ extern "C" int fqsb_set_random_forcing(fqsb_system* h, double mean, double stdde
     d.th_next = next;
     d.th_dinc = di;
     d.th_cnt = cnt;
+    d.th_list = list;
     d.th = th;
     d.th_mean = mean;
     d.th_sc = stddev * M_SQRT2; /* the association of the reference's normal transform */

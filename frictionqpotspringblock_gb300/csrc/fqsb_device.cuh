@@ -132,7 +132,8 @@ struct Ctl {
 struct Thermal {
     uint64_t state;
     uint64_t inc;
-    uint64_t base;
+    uint64_t base;  /* state before the current draw */
+    int64_t total;  /* draws of the current draw */
     uint32_t ticket;
     uint32_t pad;
 };
@@ -216,6 +217,7 @@ struct DevSys {
     int64_t* th_next;   /* next increment at which particle p redraws */
     const int64_t* th_dinc;
     int64_t* th_cnt;    /* per 1024-particle tile: draws, then their exclusive prefix */
+    int32_t* th_list;   /* the drawing particles in flat order (capacity N) */
     Thermal* th;
     double th_mean, th_sc; /* mean and stddev * sqrt(2) (rounded as the reference's normal transform) */
 };

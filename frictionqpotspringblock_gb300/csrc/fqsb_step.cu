@@ -782,9 +782,10 @@ __global__ void __launch_bounds__(128) k_regen(DevSys s)
  * takes the next draw of one pcg32 stream, f_thermal[p] = mean + (stddev sqrt 2) erfinv(2 r - 1)
  * (r = u32 2^-32), and next[p] += dinc[p].  The draws are numbered by an exclusive scan over the flat
  * index: k_th_count counts each 1024-particle tile's draws and its last CTA turns the counts into
- * tile offsets and jumps the stream past the whole draw; k_th_draw gives the particle with rank k
- * the k-th output after the old state (one jump per thread, then single steps), so the result equals
- * the reference's sequential loop.
+ * tile offsets and jumps the stream past the whole draw; k_th_list writes each drawing particle to
+ * its rank in a compact list; k_th_eval gives list entry k the k-th output after the old state (a
+ * jump-ahead per entry) with one thread per draw, so the erfinv work is dense whatever the fraction
+ * of particles that draw, and the result equals the reference's sequential loop.
  *
  * from_ctl = 1: inside a run, for the step about to run (inc = Ctl::inc + 1); nothing happens once the
  * run is over or when the run's iterations are not time steps.  from_ctl = 0: at inc = inc_arg.
@@ -881,12 +882,13 @@ __global__ void __launch_bounds__(256) k_th_count(DevSys s, int from_ctl, int64_
         Thermal* th = s.th;
         uint64_t base = th->state;
         th->base = base;
+        th->total = all;
         th->state = pcg_advance_inc(base, (uint64_t)all, th->inc);
         th->ticket = 0u;
     }
 }
 
-__global__ void __launch_bounds__(256) k_th_draw(DevSys s, int from_ctl, int64_t inc_arg)
+__global__ void __launch_bounds__(256) k_th_list(DevSys s, int from_ctl, int64_t inc_arg)
 {
     __shared__ int64_t sh8[8];
     int64_t inc;
@@ -903,26 +905,36 @@ __global__ void __launch_bounds__(256) k_th_draw(DevSys s, int from_ctl, int64_t
         n += draw[j] ? 1 : 0;
     }
     int64_t tile_total;
-    const int64_t k = s.th_cnt[blockIdx.x] + cta_exclusive_scan256(n, sh8, &tile_total);
-    if (n == 0) {
-        return;
-    }
-    const uint64_t sinc = s.th->inc;
-    uint64_t st = pcg_advance_inc(s.th->base, (uint64_t)k, sinc); /* state before draw number k */
+    int64_t k = s.th_cnt[blockIdx.x] + cta_exclusive_scan256(n, sh8, &tile_total);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-        if (!draw[j]) {
-            continue;
+        if (draw[j]) {
+            s.th_list[k++] = (int32_t)(p0 + j);
         }
-        int64_t p = p0 + j;
-        uint32_t u32 = pcg_output(st);
-        st = st * PCG_MULT + sinc;
-        double r = FQ_MUL((double)u32, 0x1p-32);
-        double z = fq_erfinv(FQ_SUB(FQ_MUL(2.0, r), 1.0));
+    }
+}
+
+/* One thread per draw: entry k of the list takes output k of the stream after the old state. */
+__global__ void __launch_bounds__(128) k_th_eval(DevSys s, int from_ctl, int64_t inc_arg)
+{
+    int64_t inc;
+    if (!th_draw_inc(s, from_ctl, inc_arg, inc)) {
+        return;
+    }
+    const int64_t total = s.th->total;
+    const uint64_t base = s.th->base, sinc = s.th->inc;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t p = s.th_list[k];
+        const uint32_t u32 = pcg_output(pcg_advance_inc(base, (uint64_t)k, sinc));
+        const double r = FQ_MUL((double)u32, 0x1p-32);
+        const double z = fq_erfinv(FQ_SUB(FQ_MUL(2.0, r), 1.0));
         s.f_th[p] = FQ_ADD(s.th_mean, FQ_MUL(s.th_sc, z));
         s.th_next[p] += s.th_dinc[p];
     }
 }
+
+/* CTAs of k_th_eval: one wave at its 138 registers (3 CTAs of 128 threads per SM), grid-stride over the draws */
+constexpr unsigned TH_EVAL_CTAS = 3 * 152;
 
 cudaError_t launch_thermal_draw(const DevSys& s, int from_ctl, int64_t inc, cudaStream_t st)
 {
@@ -930,7 +942,10 @@ cudaError_t launch_thermal_draw(const DevSys& s, int from_ctl, int64_t inc, cuda
     void* args[] = {(void*)&s, (void*)&from_ctl, (void*)&inc};
     cudaError_t e = cudaLaunchKernel((void*)k_th_count, dim3(G), dim3(256), args, 0, st);
     if (e == cudaSuccess) {
-        e = cudaLaunchKernel((void*)k_th_draw, dim3(G), dim3(256), args, 0, st);
+        e = cudaLaunchKernel((void*)k_th_list, dim3(G), dim3(256), args, 0, st);
+    }
+    if (e == cudaSuccess) {
+        e = cudaLaunchKernel((void*)k_th_eval, dim3(TH_EVAL_CTAS), dim3(128), args, 0, st);
     }
     return e;
 }
@@ -1712,11 +1727,12 @@ cudaError_t build_run_graph(DevSys& s, const LineGeom& g0, cudaGraphExec_t* exec
     void* argst[] = {(void*)&s, (void*)&th_from_ctl, (void*)&th_inc};
     if (s.f_th) {
         /* updated_inc of the step: thermal draws before the step's forces */
-        cudaGraphNode_t ncount, ndraw;
+        cudaGraphNode_t ncount, nlist, neval;
         dim3 gth((unsigned)thermal_tiles(s.N));
         GR(add_kernel(&ncount, body, nullptr, 0, (void*)k_th_count, gth, dim3(256), argst));
-        GR(add_kernel(&ndraw, body, &ncount, 1, (void*)k_th_draw, gth, dim3(256), argst));
-        GR(add_kernel(&nstep, body, &ndraw, 1, fstep, grid, block, args1));
+        GR(add_kernel(&nlist, body, &ncount, 1, (void*)k_th_list, gth, dim3(256), argst));
+        GR(add_kernel(&neval, body, &nlist, 1, (void*)k_th_eval, dim3(TH_EVAL_CTAS), dim3(128), argst));
+        GR(add_kernel(&nstep, body, &neval, 1, fstep, grid, block, args1));
     }
     else if (s.inter == INTER_LONGRANGE1D) {
         /* all new positions before the all-pairs interaction */

@@ -128,3 +128,18 @@ def test_erfinv_correctly_rounded():
     assert O.math("erfinv", 0.0) == 0.0
     assert O.math("erfinv", 1.0) == np.inf and O.math("erfinv", -1.0) == -np.inf
     assert np.isnan(O.math("erfinv", 1.5))
+
+
+def test_erfinv_correctly_rounded_whole_domain():
+    """fq_erfinv beyond the forcing grid: uniform inputs, 1 - y down to 2^-53 (x up to 5.86, the end of its
+    erf table), magnitudes down to the subnormals (the a sqrt(pi)/2 branch below 2^-500), and the
+    table's branch points."""
+    mp = pytest.importorskip("mpmath")
+    mp.mp.dps = 40
+    rng = np.random.default_rng(11)
+    ys = np.concatenate([rng.uniform(-1, 1, 500), 1 - 10 ** rng.uniform(-16, -1, 500),
+                         -(10 ** rng.uniform(-320, -1, 500)),
+                         [2.0 ** -500, 2.0 ** -499, 1e-200, 5e-324, 2.2250738585072014e-308, 1 - 2.0 ** -53,
+                          0.5, np.nextafter(0.5, 1.0), np.nextafter(0.5, 0.0), 2.0 ** -26]])
+    for y in ys:
+        assert O.math("erfinv", float(y)) == float(mp.erfinv(mp.mpf(float(y)))), y
