@@ -10,6 +10,67 @@ import re
 import sys
 
 
+def _split_top(body):
+    """Split a call's argument text at its top-level commas."""
+    parts, depth, cur = [], 0, ""
+    for ch in body:
+        if ch in "(<{":
+            depth += 1
+        elif ch in ")>}":
+            depth -= 1
+        if ch == "," and depth == 0:
+            parts.append(cur)
+            cur = ""
+        else:
+            cur += ch
+    parts.append(cur)
+    return [x.strip() for x in parts]
+
+
+def _literal(text):
+    text = text.strip()
+    if text in ("true", "false"):
+        return text == "true"
+    m = re.fullmatch(r"size_t\((.*)\)", text)
+    if m:
+        return int(float(m.group(1)))
+    v = float(text)
+    return int(v) if re.fullmatch(r"-?\d+", text) else v
+
+
+def signatures(src):
+    """py::arg names and defaults of every cls.def: methods by name, constructors by class."""
+    methods, constructors = {}, {}
+    cur, name = None, None
+    pos = 0
+    marks = []
+    for m in re.finditer(r'def_submodule\("([A-Za-z0-9]+)"|py::class_<S>\s+cls\(sm,\s*"([A-Za-z_0-9]+)"\)', src):
+        marks.append((m.start(), m.group(1), m.group(2)))
+    for m in re.finditer(r"cls\.def\(", src):
+        i, depth, j = m.end(), 1, m.end()
+        while depth:
+            depth += {"(": 1, ")": -1}.get(src[j], 0)
+            j += 1
+        for k, sub, cl in marks:
+            if k > m.start():
+                break
+            if sub:
+                cur = sub
+            if cl:
+                name = f"{cur}.{cl}"
+        parts = _split_top(src[i:j - 1])
+        args = []
+        for part in parts:
+            a = re.fullmatch(r'py::arg\("([A-Za-z_0-9]+)"\)(?:\s*=\s*(.*))?', part, re.S)
+            if a:
+                args.append([a.group(1), None if a.group(2) is None else _literal(a.group(2))])
+        if parts[0].startswith("py::init"):
+            constructors[name] = args
+        elif parts[0].startswith('"'):
+            methods[parts[0].strip('"')] = args
+    return methods, constructors
+
+
 def main():
     ref = pathlib.Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
     src = (ref / "python" / "main.cpp").read_text()
@@ -36,9 +97,11 @@ def main():
                                                            b.group(2))))
     members = sorted(set(re.findall(r'cls\.def(?:_property(?:_readonly)?)?\(\s*"([A-Za-z_0-9]+)"', src)) -
                      {"__repr__"})
+    methods, constructors = signatures(src)
     out = pathlib.Path(__file__).parent / "api_names.json"
     out.write_text(json.dumps({"classes": classes, "members": members, "binders": binders,
-                               "binder_members": binder_members}, indent=1, sort_keys=True) + "\n")
+                               "binder_members": binder_members, "methods": methods,
+                               "constructors": constructors}, indent=1, sort_keys=True) + "\n")
     print(out, sum(len(v) for v in classes.values()), "classes", len(members), "members")
 
 

@@ -47,3 +47,34 @@ def test_external_members():
     c = fqsb.detail.RandomNormalForcing_1
     for m in ("state", "f_thermal", "next"):
         assert hasattr(c, m), m
+
+
+def _check_signature(fn, expected, what):
+    import inspect
+
+    params = [p for p in inspect.signature(fn).parameters.values() if p.name != "self"]
+    named = [p for p in params if p.kind in (p.POSITIONAL_OR_KEYWORD, p.KEYWORD_ONLY)]
+    assert [p.name for p in named[:len(expected)]] == [a for a, _ in expected], what
+    for p, (name, default) in zip(named, expected):
+        if default is None:
+            assert p.default is inspect.Parameter.empty, (what, name)
+        else:
+            assert p.default == default, (what, name, p.default, default)
+    for p in named[len(expected):]:
+        assert p.default is not inspect.Parameter.empty, (what, "extra parameter without default", p.name)
+
+
+@pytest.mark.parametrize("qualified", SYSTEMS)
+def test_constructor_arguments(qualified):
+    """Argument names, order and defaults of the constructors (py::init bindings of main.cpp)."""
+    _check_signature(_cls(qualified).__init__, NAMES["constructors"][qualified], qualified)
+
+
+@pytest.mark.parametrize("qualified", SYSTEMS)
+def test_method_arguments(qualified):
+    """Argument names, order and defaults of the bound methods (the binders' py::arg lists)."""
+    c = _cls(qualified)
+    for b in NAMES["binders"][qualified]:
+        for m in NAMES["binder_members"][b]:
+            if m in NAMES["methods"] and callable(getattr(c, m, None)) and not isinstance(getattr(c, m), property):
+                _check_signature(getattr(c, m), NAMES["methods"][m], f"{qualified}.{m}")
