@@ -70,7 +70,7 @@ def build(force: bool = False, verbose: bool = False) -> pathlib.Path:
     with ThreadPoolExecutor(max_workers=len(sources())) as ex:
         objs = list(ex.map(compile_one, sources()))
     tmp = BUILD / f"libfqsb.{os.getpid()}.so"
-    cmd = [exe] + ARCH + ["-shared", "-o", str(tmp)] + [str(o) for o in objs] + ["-lcudart"]
+    cmd = [exe] + ARCH + ["-shared", "-o", str(tmp)] + [str(o) for o in objs] + ["-lcudart", "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

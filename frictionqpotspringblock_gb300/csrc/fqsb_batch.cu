@@ -777,6 +777,7 @@ static cudaError_t balloc(fqsb_batch* h, T** p, size_t count)
 
 extern "C" int fqsb_batch_create(const fqsb_batch_config* c, fqsb_batch** out)
 {
+    FQSB_API_RANGE();
     if (!c || !out || c->n_instances < 1 || !c->sizes || !c->seeds || !c->k_frame) {
         return berr(nullptr, FQSB_ERR_INVALID, "invalid batch configuration");
     }
@@ -990,6 +991,7 @@ extern "C" int fqsb_batch_quasistatic(fqsb_batch* h, int64_t ncycles, double eps
                                       uint64_t max_iter, double* u_frame_out, double* f_frame_out, int64_t* S_out,
                                       int64_t* inc_out, int32_t* status_out)
 {
+    FQSB_API_RANGE();
     if (!h || ncycles < 1 || !u_frame_out || !f_frame_out || !S_out || !inc_out || !status_out) {
         return FQSB_ERR_INVALID;
     }

@@ -791,6 +791,7 @@ static void free_all(fqsb_system* h)
 
 extern "C" int fqsb_create(const fqsb_config* cfg, fqsb_system** out)
 {
+    FQSB_API_RANGE();
     if (!cfg || !out) {
         return set_err(nullptr, FQSB_ERR_INVALID, "null argument");
     }
@@ -1054,6 +1055,7 @@ extern "C" int fqsb_get_stream(fqsb_system* h, void** stream)
 
 extern "C" int fqsb_time_steps(fqsb_system* h, uint64_t n)
 {
+    FQSB_API_RANGE();
     if (!h) {
         return FQSB_ERR_INVALID;
     }
@@ -1068,6 +1070,7 @@ extern "C" int fqsb_time_step(fqsb_system* h)
 
 extern "C" int fqsb_flow_steps(fqsb_system* h, uint64_t n, double v_frame)
 {
+    FQSB_API_RANGE();
     if (!h) {
         return FQSB_ERR_INVALID;
     }
@@ -1078,6 +1081,7 @@ extern "C" int fqsb_flow_steps(fqsb_system* h, uint64_t n, double v_frame)
 extern "C" int fqsb_time_steps_until_event(fqsb_system* h, double tol, uint64_t niter_tol, uint64_t max_iter,
                                            uint64_t* ret)
 {
+    FQSB_API_RANGE();
     if (!h || !ret) {
         return FQSB_ERR_INVALID;
     }
@@ -1145,6 +1149,7 @@ static int minimise_common(fqsb_system* h, const int64_t* i_n, uint64_t A, uint6
 extern "C" int fqsb_minimise(fqsb_system* h, double tol, uint64_t niter_tol, uint64_t max_iter, int time_activity,
                              int max_iter_is_error, uint64_t* ret)
 {
+    FQSB_API_RANGE();
     return minimise_common(h, nullptr, 0, 0, tol, niter_tol, max_iter, time_activity, max_iter_is_error, false, ret);
 }
 
@@ -1152,6 +1157,7 @@ extern "C" int fqsb_minimise_truncate(fqsb_system* h, const int64_t* i_n, uint64
                                       double tol, uint64_t niter_tol, uint64_t max_iter, int time_activity,
                                       int max_iter_is_error, uint64_t* ret)
 {
+    FQSB_API_RANGE();
     if (!i_n) {
         return FQSB_ERR_INVALID;
     }
@@ -1173,6 +1179,7 @@ __global__ void k_damping_only(DevSys d, const double* v, double* f_damp)
 extern "C" int fqsb_minimise_nopassing(fqsb_system* h, double tol, uint64_t niter_tol, uint64_t max_iter,
                                        int max_iter_is_error, uint64_t* ret)
 {
+    FQSB_API_RANGE();
     if (!h || !ret) {
         return FQSB_ERR_INVALID;
     }
@@ -1278,6 +1285,7 @@ static int advance_uniformly(fqsb_system* h, double du, double* du_frame_out)
 
 extern "C" int fqsb_event_driven_step(fqsb_system* h, double eps, int kick, int direction, double* ret)
 {
+    FQSB_API_RANGE();
     if (!h || !ret) {
         return FQSB_ERR_INVALID;
     }
@@ -1347,6 +1355,7 @@ extern "C" int fqsb_trigger(fqsb_system* h, int64_t p, double eps, int direction
 
 extern "C" int fqsb_advance_to_fixed_force(fqsb_system* h, double f_frame, int allow_plastic)
 {
+    FQSB_API_RANGE();
     if (!h) {
         return FQSB_ERR_INVALID;
     }
@@ -1421,6 +1430,7 @@ extern "C" int fqsb_refresh(fqsb_system* h)
 extern "C" int fqsb_set_random_forcing(fqsb_system* h, double mean, double stddev, uint64_t seed,
                                        const int64_t* dinc_init, const int64_t* dinc)
 {
+    FQSB_API_RANGE();
     if (!h || !dinc_init || !dinc) {
         return FQSB_ERR_INVALID;
     }
@@ -1938,6 +1948,7 @@ static int copy_state(fqsb_system* h, double* dst3, bool to_buffer)
 extern "C" int fqsb_adjoint_forward(fqsb_system* h, const double* schedule, int64_t T, int64_t K, int64_t last,
                                     double* loss)
 {
+    FQSB_API_RANGE();
     if (!h || !schedule || !loss || T < 1 || K < 1 || last < 1 || last > T) {
         return FQSB_ERR_INVALID;
     }
@@ -2013,6 +2024,7 @@ __global__ void k_adj_init(const double* uT, int64_t N, double* lu, double* lv, 
 extern "C" int fqsb_adjoint_backward(fqsb_system* h, double* grad_u0, double* grad_v0, double* grad_schedule,
                                      double* grad_params)
 {
+    FQSB_API_RANGE();
     if (!h || !grad_u0 || !grad_v0 || !grad_schedule || !grad_params) {
         return FQSB_ERR_INVALID;
     }

@@ -5,6 +5,7 @@
 #ifndef FQSB_INTERNAL_H
 #define FQSB_INTERNAL_H
 
+#include <nvtx3/nvToolsExt.h>
 #include <cuda_runtime.h>
 
 #include <string>
@@ -66,6 +67,22 @@ int64_t thermal_tiles(int64_t N);
 
 /* One loop iteration launched kernel by kernel by the host (s.in_graph must be 0). */
 cudaError_t launch_iteration(const DevSys& s, const LineGeom& g, cudaStream_t st);
+
+/* NVTX range over one C-ABI call: each stepping / construction call shows as a named range on a
+ * profiler timeline (header-only NVTX 3; a no-op unless a tool is attached). */
+struct ApiRange {
+    explicit ApiRange(const char* name)
+    {
+        nvtxRangePushA(name);
+    }
+    ~ApiRange()
+    {
+        nvtxRangePop();
+    }
+    ApiRange(const ApiRange&) = delete;
+    ApiRange& operator=(const ApiRange&) = delete;
+};
+#define FQSB_API_RANGE() fqsb::ApiRange fqsb_api_range_(__func__)
 
 /* Arguments of one backward step of the adjoint (fqsb_adjoint.cu). */
 struct AdjArgs {
