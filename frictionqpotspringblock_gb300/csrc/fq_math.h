@@ -424,32 +424,28 @@ FQ_HD double fq_cos(double x)
  * For the normal quantile of thermal forcing, mean + stddev sqrt(2) erfinv(2 r - 1).
  *
  * erf near a grid point.  With x_i = i/64 and G_i = (2/sqrt(pi)) exp(-x_i^2),
- *     (2/sqrt(pi)) exp(-(x_i + h)^2) = G_i sum_k p_k h^k,   p_0 = 1, p_1 = -2 x_i,
- *     (k + 1) p_{k+1} = -2 x_i p_k - 2 p_{k-1}               (Taylor series of exp(-2 x_i h - h^2)),
- * so erf(x_i + h) = erf(x_i) + G_i S(h) and erfc(x_i + h) = erfc(x_i) - G_i S(h) with
- * S(h) = sum_k p_k h^(k+1) / (k+1).  erf(x_i), erfc(x_i) and G_i come as double-doubles from a table
- * (fq_erf_table.h, 60-digit mpmath); with |h| <= 1/128, 16 terms leave a truncation error below
- * 1e-29 relative to G_i, so the double-double sum resolves erfc(x) to ~1e-27 relative up to x = 6.
+ *     erf(x_i + h) = erf(x_i) + G_i S(h),  erfc(x_i + h) = erfc(x_i) - G_i S(h),
+ *     S(h) = sum_k q_k h^(k+1),  q_k = p_k / (k+1),  sum_k p_k h^k = exp(-2 x_i h - h^2),
+ * the Taylor series of erf's derivative about x_i (p_k = (-1)^k H_k(x_i) / k!).  erf(x_i), erfc(x_i),
+ * G_i and q_0 .. q_15 come from a table (fq_erf_table.h, 60-digit mpmath; the leading coefficients as
+ * double-doubles).  With |h| <= 1/128 the truncation error is below 1e-29 relative to G_i, so the
+ * double-double sum resolves erfc(x) to ~1e-27 relative up to x = 6.
  *
  * erfinv(y): bracket |y| (or 1 - |y| > 1/2, which is exact, against erfc) in the table, interpolate
- * linearly (error <= 4e-4), then three Halley steps x -= d / (1 + x d), d = residual / derivative: the
- * first with a double residual (error ~1e-9 after it), the last two with the double-double residual.
- * The last step's correction is below an ulp and is computed to ~16 digits, so the result is the
- * correctly rounded erfinv except within ~1e-16 ulp of a rounding midpoint.  Host and device run the
- * same code (the table is duplicated into device memory), so they agree bit for bit.
+ * linearly (error <= 4e-4), then Halley steps x -= d / (1 + x d), d = residual / derivative: two with a
+ * double residual (to ~1 ulp), the last with the double-double residual.  That last correction is about
+ * an ulp and is computed to ~16 digits, so the result is the correctly rounded erfinv except within
+ * ~1e-16 ulp of a rounding midpoint.  Host and device run the same code (the table is duplicated into
+ * device memory), so they agree bit for bit.
  */
 #include "fq_erf_table.h"
 
-#define FQ_ERF_K 16
-
 #if defined(__CUDACC__)
-__device__ static const double fq_erf_tab_dev[FQ_ERF_N][6] = FQ_ERF_TABLE_INIT;
-__device__ static const double fq_inv_tab_dev[FQ_INV_N][2] = FQ_INV_TABLE_INIT;
+__device__ static const double fq_erf_tab_dev[FQ_ERF_N][FQ_ERF_ROW] = FQ_ERF_TABLE_INIT;
 #endif
-static const double fq_erf_tab_host[FQ_ERF_N][6] = FQ_ERF_TABLE_INIT;
-static const double fq_inv_tab_host[FQ_INV_N][2] = FQ_INV_TABLE_INIT;
+static const double fq_erf_tab_host[FQ_ERF_N][FQ_ERF_ROW] = FQ_ERF_TABLE_INIT;
 
-/* row i of the erf table: erf hi, lo, erfc hi, lo, G hi, lo */
+/* row i of the erf table: erf (hi, lo), erfc (hi, lo), G (hi, lo), q_0 .. q_7 (hi, lo), q_8 .. q_15 */
 FQ_HD const double* fq_erf_row(int i)
 {
 #if defined(__CUDA_ARCH__)
@@ -459,30 +455,10 @@ FQ_HD const double* fq_erf_row(int i)
 #endif
 }
 
-/* 1/k as a double-double, 1 <= k < FQ_INV_N */
-FQ_HD fq_dd fq_inv_k(int k)
+/* q_k of a row, rounded to double */
+FQ_HD double fq_erf_q(const double* row, int k)
 {
-#if defined(__CUDA_ARCH__)
-    return fq_dd_make(fq_inv_tab_dev[k][0], fq_inv_tab_dev[k][1]);
-#else
-    return fq_dd_make(fq_inv_tab_host[k][0], fq_inv_tab_host[k][1]);
-#endif
-}
-
-/* Coefficients of grid point i: q_k = p_k / (k+1) (double-double) and p_k (double). */
-FQ_HD void fq_erf_coeffs(int i, fq_dd* q, double* p)
-{
-    const double m2x = FQ_MUL(-(double)i, 0x1p-5); /* -2 x_i, exact */
-    fq_dd pm = fq_dd_make(0.0, 0.0);
-    fq_dd pk = fq_dd_make(1.0, 0.0);
-    for (int k = 0; k < FQ_ERF_K; ++k) {
-        const fq_dd inv = fq_inv_k(k + 1);
-        p[k] = pk.hi;
-        q[k] = fq_dd_mul(pk, inv);
-        fq_dd t = fq_dd_add(fq_dd_mul_d(pk, m2x), fq_dd_make(FQ_MUL(-2.0, pm.hi), FQ_MUL(-2.0, pm.lo)));
-        pm = pk;
-        pk = fq_dd_mul(t, inv);
-    }
+    return k < FQ_ERF_K_DD ? row[6 + 2 * k] : row[6 + 2 * FQ_ERF_K_DD + (k - FQ_ERF_K_DD)];
 }
 
 /* nearest grid point of x >= 0 */
@@ -537,40 +513,37 @@ FQ_HD double fq_erfinv(double y)
     t = t < 0.0 ? 0.0 : (t > 1.0 ? 1.0 : t);
     double x = FQ_MUL(FQ_ADD((double)lo, t), 0x1p-6);
 
-    fq_dd qk[FQ_ERF_K];
-    double pk[FQ_ERF_K];
-    int cell = fq_erf_cell(x);
-    fq_erf_coeffs(cell, qk, pk);
     for (int it = 0; it < 3; ++it) {
-        const int c = fq_erf_cell(x);
-        if (c != cell) {
-            cell = c;
-            fq_erf_coeffs(cell, qk, pk);
-        }
+        const int cell = fq_erf_cell(x);
         const double* row = fq_erf_row(cell);
         const double h = FQ_SUB(x, FQ_MUL((double)cell, 0x1p-6)); /* exact */
         double r;
-        if (it == 0) {
-            double s = qk[FQ_ERF_K - 1].hi;
+        if (it < 2) {
+            double s = fq_erf_q(row, FQ_ERF_K - 1);
             for (int k = FQ_ERF_K - 2; k >= 0; --k) {
-                s = FQ_ADD(FQ_MUL(s, h), qk[k].hi);
+                s = FQ_ADD(FQ_MUL(s, h), fq_erf_q(row, k));
             }
             const double gs = FQ_MUL(row[4], FQ_MUL(s, h));
             r = tail ? FQ_SUB(FQ_SUB(row[2], gs), q) : FQ_SUB(FQ_ADD(row[0], gs), a);
         }
         else {
-            fq_dd s = qk[FQ_ERF_K - 1];
-            for (int k = FQ_ERF_K - 2; k >= 0; --k) {
-                s = fq_dd_add(fq_dd_mul_d(s, h), qk[k]);
+            double s = fq_erf_q(row, FQ_ERF_K - 1);
+            for (int k = FQ_ERF_K - 2; k >= FQ_ERF_K_DD; --k) {
+                s = FQ_ADD(FQ_MUL(s, h), fq_erf_q(row, k));
             }
-            const fq_dd gs = fq_dd_mul(fq_dd_make(row[4], row[5]), fq_dd_mul_d(s, h));
+            fq_dd S = fq_dd_make(s, 0.0);
+            for (int k = FQ_ERF_K_DD - 1; k >= 0; --k) {
+                S = fq_dd_add(fq_dd_mul_d(S, h), fq_dd_make(row[6 + 2 * k], row[7 + 2 * k]));
+            }
+            const fq_dd gs = fq_dd_mul(fq_dd_make(row[4], row[5]), fq_dd_mul_d(S, h));
             const fq_dd v = tail ? fq_dd_add(fq_dd_make(row[2], row[3]), fq_dd_neg(gs))
                                  : fq_dd_add(fq_dd_make(row[0], row[1]), gs);
             r = FQ_ADD(FQ_SUB(v.hi, target), v.lo);
         }
-        double g = pk[FQ_ERF_K - 1];
+        /* derivative (2/sqrt(pi)) exp(-x^2) = G sum_k (k+1) q_k h^k */
+        double g = FQ_MUL((double)FQ_ERF_K, fq_erf_q(row, FQ_ERF_K - 1));
         for (int k = FQ_ERF_K - 2; k >= 0; --k) {
-            g = FQ_ADD(FQ_MUL(g, h), pk[k]);
+            g = FQ_ADD(FQ_MUL(g, h), FQ_MUL((double)(k + 1), fq_erf_q(row, k)));
         }
         const double deriv = FQ_MUL(row[4], g);
         const double d = tail ? FQ_DIV(-r, deriv) : FQ_DIV(r, deriv);

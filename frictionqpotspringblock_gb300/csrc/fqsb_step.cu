@@ -933,8 +933,8 @@ __global__ void __launch_bounds__(128) k_th_eval(DevSys s, int from_ctl, int64_t
     }
 }
 
-/* CTAs of k_th_eval: one wave at its 138 registers (3 CTAs of 128 threads per SM), grid-stride over the draws */
-constexpr unsigned TH_EVAL_CTAS = 3 * 152;
+/* CTAs of k_th_eval (72 registers, 128 threads): 4 per SM, 78 k draws per pass, grid-stride beyond */
+constexpr unsigned TH_EVAL_CTAS = 4 * 152;
 
 cudaError_t launch_thermal_draw(const DevSys& s, int from_ctl, int64_t inc, cudaStream_t st)
 {
