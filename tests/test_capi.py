@@ -96,3 +96,50 @@ int main()
     inc = pathlib.Path(__file__).resolve().parent.parent / "include"
     r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", f"-I{inc}", str(src)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_c_program_links_and_calls(tmp_path):
+    """A plain C caller (the binding a non-Python code base would add) links libfqsb.so, reads the
+    version and gets the documented status and message from fqsb_create without a GPU."""
+    import shutil
+    import subprocess
+
+    import torch
+
+    if shutil.which("gcc") is None:
+        pytest.skip("needs gcc")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present (the program expects FQSB_ERR_NO_DEVICE)")
+    from frictionqpotspringblock_gb300 import _build_lib
+
+    lib = _build_lib.build()
+    src = tmp_path / "caller.c"
+    src.write_text(r"""
+#include <stdio.h>
+#include <string.h>
+#include "fqsb.h"
+int main(void)
+{
+    fqsb_config cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cfg.potential = FQSB_CUSPY; cfg.interactions = FQSB_LAPLACE1D; cfg.rows = 1; cfg.cols = 1024;
+    cfg.m = 1; cfg.eta = 0.1; cfg.mu = 1; cfg.k_interactions = 1; cfg.k_frame = 1.0 / 1024; cfg.dt = 0.1;
+    cfg.distribution = FQSB_DIST_WEIBULL; cfg.n_parameters = 3;
+    cfg.parameters[0] = 2; cfg.parameters[1] = 1; cfg.parameters[2] = 1e-5;
+    cfg.offset = -100; cfg.nchunk = 100;
+    fqsb_system* h = NULL;
+    int rc = fqsb_create(&cfg, &h);
+    printf("%s|%d|%s|%d\n", fqsb_version(), rc, fqsb_last_error(NULL), h == NULL);
+    return 0;
+}
+""")
+    exe = tmp_path / "caller"
+    inc = ROOT / "include"
+    r = subprocess.run(["gcc", "-std=c11", f"-I{inc}", str(src), "-o", str(exe), f"-L{lib.parent}", "-lfqsb",
+                        f"-Wl,-rpath,{lib.parent}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    version, rc, msg, null = r.stdout.strip().split("|")
+    assert version.endswith("sm_103a")
+    assert int(rc) == 9 and "no CUDA device" in msg and null == "1"
