@@ -143,3 +143,19 @@ def test_erfinv_correctly_rounded_whole_domain():
                           0.5, np.nextafter(0.5, 1.0), np.nextafter(0.5, 0.0), 2.0 ** -26]])
     for y in ys:
         assert O.math("erfinv", float(y)) == float(mp.erfinv(mp.mpf(float(y)))), y
+
+
+def test_erf_table_matches_its_generator():
+    """csrc/fq_erf_table.h is exactly what csrc/gen_erf_table.py writes (60-digit mpmath)."""
+    pytest.importorskip("mpmath")
+    import importlib.util
+    import io
+    import pathlib
+
+    csrc = pathlib.Path(__file__).resolve().parent.parent / "frictionqpotspringblock_gb300" / "csrc"
+    spec = importlib.util.spec_from_file_location("gen_erf_table", csrc / "gen_erf_table.py")
+    gen = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(gen)
+    out = io.StringIO()
+    gen.main(out)
+    assert out.getvalue() == (csrc / "fq_erf_table.h").read_text()
