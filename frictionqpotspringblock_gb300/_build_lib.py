@@ -20,7 +20,7 @@ CSRC = HERE / "csrc"
 BUILD = HERE / "_build"
 LIB = BUILD / "libfqsb.so"
 INCLUDE = HERE.parent / "include"
-UNITS = ["fqsb_capi.cu", "fqsb_step.cu", "fqsb_noalloc.cu", "fqsb_batch.cu", "fqsb_adjoint.cu"]
+UNITS = ["fqsb_capi.cu", "fqsb_step.cu", "fqsb_noalloc.cu", "fqsb_batch.cu", "fqsb_adjoint.cu", "fqsb_measure.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

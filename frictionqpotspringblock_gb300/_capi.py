@@ -142,6 +142,7 @@ SIGNATURES = [
     ("fqsb_random_forcing_set", _I, [_P, _PU64, _PD, _PI64]),
     ("fqsb_adjoint_forward", _I, [_P, _PD, _I64, _I64, _I64, _PD]),
     ("fqsb_adjoint_backward", _I, [_P, _PD, _PD, _PD, _PD]),
+    ("fqsb_adjoint_backward_device", _I, [_P, _P, _P, _PD, _PD]),
     ("fqsb_batch_create", _I, [ctypes.POINTER(BatchConfig), ctypes.POINTER(_P)]),
     ("fqsb_batch_destroy", _I, [_P]),
     ("fqsb_batch_last_error", ctypes.c_char_p, [_P]),
@@ -149,6 +150,7 @@ SIGNATURES = [
     ("fqsb_batch_get", _I, [_P, _I64, _I, _PD]),
     ("fqsb_batch_get_index", _I, [_P, _I64, _PI64]),
     ("fqsb_batch_frame", _I, [_P, _PD]),
+    ("fqsb_measure_arith", _I, [_I, _I, _I, _PD]),
     ("fqsb_version", ctypes.c_char_p, []),
 ]
 
@@ -171,6 +173,15 @@ def lib() -> ctypes.CDLL:
             fn.argtypes = args
         _lib = L
     return _lib
+
+
+def measure_arith(op: str = "add", n_soft: int = 0, device: int = 0) -> float:
+    """Binary64 operations per second (Gop/s) of this GPU for op "add", "mul" or "fma", with n_soft of
+    8 independent chains per thread in the integer-pipe form of the step kernels (fqsb_measure_arith)."""
+    out = ctypes.c_double()
+    check(None, lib().fqsb_measure_arith(int(device), {"add": 0, "mul": 1, "fma": 2}[op], int(n_soft),
+                                         ctypes.byref(out)))
+    return out.value
 
 
 def exported_symbols() -> list[str]:

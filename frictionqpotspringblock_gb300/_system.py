@@ -207,6 +207,7 @@ class System:
         if status != C.OK:
             raise C.FrictionError(status, C.lib().fqsb_last_error(None).decode())
         self._h = h
+        self._device = int(device)
         self._shape = shape
         self._size = rows * cols
         self._nchunk = int(nchunk)
@@ -417,7 +418,22 @@ class System:
                                                        _ptr(gs, ctypes.c_double), _ptr(gp, ctypes.c_double)))
         return gu.reshape(self._shape), gv.reshape(self._shape), gs, gp
 
+    def adjoint_backward_device(self, grad_u0_ptr: int, grad_v0_ptr: int):
+        """As adjoint_backward, with dL/du0 and dL/dv0 written to device arrays of N doubles on the system's
+        device (pointers as integers); returns (dL/dschedule, [dL/dmu, dL/dk_interactions, dL/deta])."""
+        gs = np.empty(self._adj_T)
+        gp = np.empty(3)
+        C.check(self._h, C.lib().fqsb_adjoint_backward_device(self._h, ctypes.c_void_p(grad_u0_ptr),
+                                                              ctypes.c_void_p(grad_v0_ptr),
+                                                              _ptr(gs, ctypes.c_double), _ptr(gp, ctypes.c_double)))
+        return gs, gp
+
     # ---------------------------------------------------------------- device access
+    @property
+    def device(self) -> int:
+        """The CUDA device ordinal the system lives on."""
+        return self._device
+
     @property
     def stream(self) -> int:
         """The cudaStream_t (as an integer) the system launches its kernels on."""

@@ -24,7 +24,9 @@
  * run on it alone -- bit for bit.
  */
 #include <algorithm>
+#include <climits>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -1001,35 +1003,55 @@ extern "C" int fqsb_batch_quasistatic(fqsb_batch* h, int64_t ncycles, double eps
     if (!(tol < 1.0)) {
         return berr(h, FQSB_ERR_INVALID, "assertion failed (tol < 1.0)");
     }
+    if (ncycles > (int64_t)INT32_MAX || (uint64_t)h->ninst > (SIZE_MAX / sizeof(double)) / (uint64_t)ncycles) {
+        return berr(h, FQSB_ERR_INVALID, "ncycles too large");
+    }
     BatchDev& b = h->b;
-    size_t nout = (size_t)(h->ninst * ncycles);
-    std::vector<void*> tmp;
-    double *du, *df;
-    int64_t *dS, *dI;
-    BCU(h, cudaMalloc(&du, sizeof(double) * nout));
-    BCU(h, cudaMalloc(&df, sizeof(double) * nout));
-    BCU(h, cudaMalloc(&dS, sizeof(int64_t) * nout));
-    BCU(h, cudaMalloc(&dI, sizeof(int64_t) * nout));
-    b.out_uframe = du;
-    b.out_fframe = df;
-    b.out_S = dS;
-    b.out_inc = dI;
-    /* the output pointers are kernel arguments: rebuild the graph for this run */
+    const size_t nout = (size_t)h->ninst * (size_t)ncycles;
+    double *du = nullptr, *df = nullptr;
+    int64_t *dS = nullptr, *dI = nullptr;
+    /* one exit path for every outcome: the output buffers are freed, and the graph (whose kernel
+     * arguments point at them) is destroyed with the pointers cleared */
+    auto release = [&]() {
+        for (void* p : {(void*)du, (void*)df, (void*)dS, (void*)dI}) {
+            if (p) {
+                cudaFree(p);
+            }
+        }
+        b.out_uframe = nullptr;
+        b.out_fframe = nullptr;
+        b.out_S = nullptr;
+        b.out_inc = nullptr;
+        if (h->graph) {
+            cudaGraphExecDestroy(h->graph);
+            h->graph = nullptr;
+        }
+    };
+#define QCU(expr)                                                                                        \
+    do {                                                                                                 \
+        cudaError_t e_ = (expr);                                                                         \
+        if (e_ != cudaSuccess) {                                                                         \
+            release();                                                                                   \
+            return berr(h, FQSB_ERR_CUDA, std::string(#expr ": ") + cudaGetErrorString(e_));             \
+        }                                                                                                \
+    } while (0)
     if (h->graph) {
         cudaGraphExecDestroy(h->graph);
         h->graph = nullptr;
     }
-    cudaError_t e = build_batch_graph(b, h->threads, &h->graph);
-    if (e != cudaSuccess) {
-        cudaFree(du);
-        cudaFree(df);
-        cudaFree(dS);
-        cudaFree(dI);
-        return berr(h, FQSB_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(e));
-    }
+    QCU(cudaMalloc(&du, sizeof(double) * nout));
+    QCU(cudaMalloc(&df, sizeof(double) * nout));
+    QCU(cudaMalloc(&dS, sizeof(int64_t) * nout));
+    QCU(cudaMalloc(&dI, sizeof(int64_t) * nout));
+    b.out_uframe = du;
+    b.out_fframe = df;
+    b.out_S = dS;
+    b.out_inc = dI;
+    /* the output pointers are kernel arguments: build the graph for this run */
+    QCU(build_batch_graph(b, h->threads, &h->graph));
     /* reset every realisation's protocol state (keeps u, v, a, wells and frame positions) */
     std::vector<Inst> inst((size_t)h->ninst);
-    BCU(h, cudaMemcpy(inst.data(), b.inst, sizeof(Inst) * inst.size(), cudaMemcpyDeviceToHost));
+    QCU(cudaMemcpy(inst.data(), b.inst, sizeof(Inst) * inst.size(), cudaMemcpyDeviceToHost));
     for (auto& I : inst) {
         I.phase = PH_EVT_MIN;
         I.cycle = 0;
@@ -1040,7 +1062,7 @@ extern "C" int fqsb_batch_quasistatic(fqsb_batch* h, int64_t ncycles, double eps
         I.s_signed = 0;
         I.min_key = 0x7ff0000000000000ULL;
     }
-    BCU(h, cudaMemcpyAsync(b.inst, inst.data(), sizeof(Inst) * inst.size(), cudaMemcpyHostToDevice, h->stream));
+    QCU(cudaMemcpyAsync(b.inst, inst.data(), sizeof(Inst) * inst.size(), cudaMemcpyHostToDevice, h->stream));
     BatchRun R;
     memset(&R, 0, sizeof(R));
     R.ncycles = (int32_t)ncycles;
@@ -1051,29 +1073,27 @@ extern "C" int fqsb_batch_quasistatic(fqsb_batch* h, int64_t ncycles, double eps
     R.max_iter = (int64_t)max_iter;
     R.active = (int32_t)h->ninst;
     R.budget_ns = 200ull * 1000ull * 1000ull;
-    BCU(h, cudaMemcpyAsync(b.run, &R, sizeof(R), cudaMemcpyHostToDevice, h->stream));
+    QCU(cudaMemcpyAsync(b.run, &R, sizeof(R), cudaMemcpyHostToDevice, h->stream));
     for (;;) {
-        BCU(h, cudaGraphLaunch(h->graph, h->stream));
-        BCU(h, cudaMemcpyAsync(&R, b.run, sizeof(R), cudaMemcpyDeviceToHost, h->stream));
-        BCU(h, cudaStreamSynchronize(h->stream));
+        QCU(cudaGraphLaunch(h->graph, h->stream));
+        QCU(cudaMemcpyAsync(&R, b.run, sizeof(R), cudaMemcpyDeviceToHost, h->stream));
+        QCU(cudaStreamSynchronize(h->stream));
         if (R.active <= 0 || R.walk_flag) {
             break;
         }
         int64_t zero = 0;
-        BCU(h, cudaMemcpyAsync(&b.run->launch_iters, &zero, sizeof(zero), cudaMemcpyHostToDevice, h->stream));
+        QCU(cudaMemcpyAsync(&b.run->launch_iters, &zero, sizeof(zero), cudaMemcpyHostToDevice, h->stream));
     }
-    BCU(h, cudaMemcpy(u_frame_out, du, sizeof(double) * nout, cudaMemcpyDeviceToHost));
-    BCU(h, cudaMemcpy(f_frame_out, df, sizeof(double) * nout, cudaMemcpyDeviceToHost));
-    BCU(h, cudaMemcpy(S_out, dS, sizeof(int64_t) * nout, cudaMemcpyDeviceToHost));
-    BCU(h, cudaMemcpy(inc_out, dI, sizeof(int64_t) * nout, cudaMemcpyDeviceToHost));
-    BCU(h, cudaMemcpy(inst.data(), b.inst, sizeof(Inst) * inst.size(), cudaMemcpyDeviceToHost));
+    QCU(cudaMemcpy(u_frame_out, du, sizeof(double) * nout, cudaMemcpyDeviceToHost));
+    QCU(cudaMemcpy(f_frame_out, df, sizeof(double) * nout, cudaMemcpyDeviceToHost));
+    QCU(cudaMemcpy(S_out, dS, sizeof(int64_t) * nout, cudaMemcpyDeviceToHost));
+    QCU(cudaMemcpy(inc_out, dI, sizeof(int64_t) * nout, cudaMemcpyDeviceToHost));
+    QCU(cudaMemcpy(inst.data(), b.inst, sizeof(Inst) * inst.size(), cudaMemcpyDeviceToHost));
+#undef QCU
+    release();
     for (size_t j = 0; j < inst.size(); ++j) {
         status_out[j] = inst[j].status;
     }
-    cudaFree(du);
-    cudaFree(df);
-    cudaFree(dS);
-    cudaFree(dI);
     if (R.walk_flag) {
         return berr(h, FQSB_ERR_TIMEOUT, "yield search exceeded its bound");
     }

@@ -2021,10 +2021,11 @@ __global__ void k_adj_init(const double* uT, int64_t N, double* lu, double* lv, 
     }
 }
 
-extern "C" int fqsb_adjoint_backward(fqsb_system* h, double* grad_u0, double* grad_v0, double* grad_schedule,
-                                     double* grad_params)
+/* The backward of fqsb_adjoint_backward / _device: grad_u0 and grad_v0 are copied out with `out_kind`
+ * (device-to-host for host buffers, device-to-device for device buffers). */
+static int adjoint_backward(fqsb_system* h, double* grad_u0, double* grad_v0, double* grad_schedule,
+                            double* grad_params, cudaMemcpyKind out_kind)
 {
-    FQSB_API_RANGE();
     if (!h || !grad_u0 || !grad_v0 || !grad_schedule || !grad_params) {
         return FQSB_ERR_INVALID;
     }
@@ -2120,8 +2121,8 @@ extern "C" int fqsb_adjoint_backward(fqsb_system* h, double* grad_u0, double* gr
         return rc;
     }
     std::vector<double> so((size_t)(4 * T));
-    ACU(cudaMemcpyAsync(grad_u0, lin, nb, cudaMemcpyDeviceToHost, h->stream));
-    ACU(cudaMemcpyAsync(grad_v0, lin + N, nb, cudaMemcpyDeviceToHost, h->stream));
+    ACU(cudaMemcpyAsync(grad_u0, lin, nb, out_kind, h->stream));
+    ACU(cudaMemcpyAsync(grad_v0, lin + N, nb, out_kind, h->stream));
     ACU(cudaMemcpyAsync(so.data(), step_out, sizeof(double) * 4 * (size_t)T, cudaMemcpyDeviceToHost, h->stream));
     ACU(cudaStreamSynchronize(h->stream));
     double gmu = 0.0, gk = 0.0, geta = 0.0;
@@ -2141,4 +2142,19 @@ extern "C" int fqsb_adjoint_backward(fqsb_system* h, double* grad_u0, double* gr
     cleanup();
 #undef ACU
     return rc ? rc : sync(h);
+}
+
+extern "C" int fqsb_adjoint_backward(fqsb_system* h, double* grad_u0, double* grad_v0, double* grad_schedule,
+                                     double* grad_params)
+{
+    FQSB_API_RANGE();
+    return adjoint_backward(h, grad_u0, grad_v0, grad_schedule, grad_params, cudaMemcpyDeviceToHost);
+}
+
+extern "C" int fqsb_adjoint_backward_device(fqsb_system* h, double* grad_u0_device, double* grad_v0_device,
+                                            double* grad_schedule, double* grad_params)
+{
+    FQSB_API_RANGE();
+    return adjoint_backward(h, grad_u0_device, grad_v0_device, grad_schedule, grad_params,
+                            cudaMemcpyDeviceToDevice);
 }

@@ -205,6 +205,10 @@ int fqsb_set_parameters(fqsb_system* h, double mu, double k_interactions, double
  */
 int fqsb_adjoint_forward(fqsb_system* h, const double* schedule, int64_t T, int64_t K, int64_t last, double* loss);
 int fqsb_adjoint_backward(fqsb_system* h, double* grad_u0, double* grad_v0, double* grad_schedule, double* grad_params);
+/* As fqsb_adjoint_backward, with dL/du_0 and dL/dv_0 written to device arrays of N doubles on the handle's
+ * device (for callers whose tensors live on the GPU); grad_schedule and grad_params stay host arrays. */
+int fqsb_adjoint_backward_device(fqsb_system* h, double* grad_u0_device, double* grad_v0_device,
+                                 double* grad_schedule, double* grad_params);
 
 /*
  * Batched form: many independent Line1d System_Cuspy_Laplace realisations of uneven size (realisation j:
@@ -265,6 +269,14 @@ int fqsb_batch_frame(fqsb_batch* h, double* u_frame); /* u_frame of every realis
 #define FQSB_NOALLOC_MAX_N ((int64_t)1 << 25)
 int fqsb_residual_noalloc(const double* f_device, const double* f_frame_device, int64_t n, double* residual_device,
                           void* stream);
+
+/*
+ * Measurement support (no counterpart in the reference): binary64 operations per second of this GPU for
+ * op = 0 (add), 1 (mul) or 2 (fma), with n_soft of 8 independent chains per thread in the integer-pipe
+ * form the step kernels use (0 = all on the fp64 pipe; fma: 0 only).  The fp64 roofline denominator of
+ * the step kernel.  Allocates and frees a small output buffer; runs two launches of ~10 ms.
+ */
+int fqsb_measure_arith(int device, int op, int n_soft, double* gops);
 
 /* Build information: "fqsb <version> sm_103a". */
 const char* fqsb_version(void);

@@ -35,6 +35,35 @@
 #include <stdlib.h>
 #include <string.h>
 
+/*
+ * Built with -fopenmp (the threaded variant timed as the CPU reference arm), the per-particle loops of
+ * construction and of timeStep run in parallel over particle ranges; every iteration is independent
+ * (reductions and the thermal draws, which follow one sequential stream, stay sequential), so the
+ * results equal the single-threaded build's bit for bit.
+ */
+#ifdef _OPENMP
+#include <omp.h>
+#define OQ_PARALLEL_FOR _Pragma("omp parallel for schedule(static)")
+static int oq_thread_id(void)
+{
+    return omp_get_thread_num();
+}
+static int oq_max_threads(void)
+{
+    return omp_get_max_threads();
+}
+#else
+#define OQ_PARALLEL_FOR
+static int oq_thread_id(void)
+{
+    return 0;
+}
+static int oq_max_threads(void)
+{
+    return 1;
+}
+#endif
+
 #define PCG_MULT 0x5851f42d4c957f2dULL
 
 struct oq_system {
@@ -303,6 +332,7 @@ static void align_p(oq_system* s, int64_t p, double u)
 {
     int64_t n = s->n;
     double* y = s->data + p * n;
+    double* blk = s->blk + (size_t)oq_thread_id() * (size_t)n; /* this thread's search block */
     int64_t li = s->cidx[p];
     int64_t gi;
     if (u != u || u == INFINITY || u == -INFINITY) {
@@ -328,9 +358,9 @@ static void align_p(oq_system* s, int64_t p, double u)
     else if (u >= y[n - 1]) {
         int64_t k = s->start[p] + n - 1; /* y_k <= u */
         for (;;) {
-            seq_fill(s, p, k + 1, n, s->blk);
+            seq_fill(s, p, k + 1, n, blk);
             int64_t j = 0;
-            while (j < n && s->blk[j] <= u) {
+            while (j < n && blk[j] <= u) {
                 ++j;
             }
             if (j < n) {
@@ -343,9 +373,9 @@ static void align_p(oq_system* s, int64_t p, double u)
     else {
         int64_t k = s->start[p]; /* y_k > u */
         for (;;) {
-            seq_fill(s, p, k - n, n, s->blk);
+            seq_fill(s, p, k - n, n, blk);
             int64_t j = n - 1;
-            while (j >= 0 && s->blk[j] > u) {
+            while (j >= 0 && blk[j] > u) {
                 --j;
             }
             if (j >= 0) {
@@ -363,6 +393,7 @@ static void align_p(oq_system* s, int64_t p, double u)
 
 static void align_all(oq_system* s)
 {
+    OQ_PARALLEL_FOR
     for (int64_t p = 0; p < s->N; ++p) {
         align_p(s, p, s->u[p]);
     }
@@ -413,6 +444,7 @@ static void compute_force_potential(oq_system* s)
 {
     int64_t N = s->N, n = s->n;
     align_all(s);
+    OQ_PARALLEL_FOR
     for (int64_t p = 0; p < N; ++p) {
         const double* y = s->data + p * n + s->cidx[p];
         double up = s->u[p];
@@ -440,6 +472,7 @@ static void compute_force_potential(oq_system* s)
         }
     }
     if (s->pot == OQ_CUSPY) {
+        OQ_PARALLEL_FOR
         for (int64_t p = 0; p < N; ++p) {
             s->f_pot[p] *= s->mu;
         }
@@ -453,11 +486,13 @@ static void compute_force_interactions(oq_system* s)
     const double* u = s->u;
     double* f = s->f_int;
     if (s->inter == OQ_LAPLACE1D) {
+        OQ_PARALLEL_FOR
         for (int64_t p = 0; p < N; ++p) {
             int64_t l = p == 0 ? N - 1 : p - 1;
             int64_t r = p == N - 1 ? 0 : p + 1;
             f[p] = u[l] - 2 * u[p] + u[r];
         }
+        OQ_PARALLEL_FOR
         for (int64_t p = 0; p < N; ++p) {
             f[p] *= s->k;
         }
@@ -524,6 +559,7 @@ static void compute_force_interactions(oq_system* s)
     }
     else if (s->inter == OQ_LAPLACE2D) {
         int64_t R = s->rows, C = s->cols;
+        OQ_PARALLEL_FOR
         for (int64_t i = 0; i < R; ++i) {
             int64_t im = (i + R - 1) % R, ip = (i + 1) % R;
             for (int64_t j = 0; j < C; ++j) {
@@ -531,6 +567,7 @@ static void compute_force_interactions(oq_system* s)
                 f[i * C + j] = u[im * C + j] + u[ip * C + j] + u[i * C + jm] + u[i * C + jp] - 4 * u[i * C + j];
             }
         }
+        OQ_PARALLEL_FOR
         for (int64_t p = 0; p < N; ++p) {
             f[p] *= s->k;
         }
@@ -540,6 +577,7 @@ static void compute_force_interactions(oq_system* s)
 /* computeForceFrame detail.h:1353-1356 */
 static void compute_force_frame(oq_system* s)
 {
+    OQ_PARALLEL_FOR
     for (int64_t p = 0; p < s->N; ++p) {
         s->f_frame[p] = s->k_frame * (s->u_frame - s->u[p]);
     }
@@ -549,6 +587,7 @@ static void compute_force_frame(oq_system* s)
 static void compute_force_damping(oq_system* s)
 {
     double me = -s->eta;
+    OQ_PARALLEL_FOR
     for (int64_t p = 0; p < s->N; ++p) {
         s->f_damp[p] = me * s->v[p];
     }
@@ -557,10 +596,12 @@ static void compute_force_damping(oq_system* s)
 /* computeForce detail.h:1321-1330 (with External: + f_thermal) */
 static void compute_force(oq_system* s)
 {
+    OQ_PARALLEL_FOR
     for (int64_t p = 0; p < s->N; ++p) {
         s->f[p] = s->f_frame[p] + s->f_pot[p] + s->f_int[p] + s->f_damp[p];
     }
     if (s->thermal) {
+        OQ_PARALLEL_FOR
         for (int64_t p = 0; p < s->N; ++p) {
             s->f[p] = s->f[p] + s->f_th[p];
         }
@@ -687,12 +728,13 @@ oq_system* oq_create(int potential, int interactions, int64_t rows, int64_t cols
     s->data = (double*)malloc(sizeof(double) * (size_t)(N * nchunk));
     s->start = (int64_t*)calloc((size_t)N, sizeof(int64_t));
     s->cidx = (int64_t*)calloc((size_t)N, sizeof(int64_t));
-    s->blk = (double*)malloc(sizeof(double) * (size_t)nchunk);
+    s->blk = (double*)malloc(sizeof(double) * (size_t)nchunk * (size_t)oq_max_threads());
     double** arrs[] = {&s->u, &s->v, &s->a, &s->v_n, &s->a_n, &s->f, &s->f_pot, &s->f_int, &s->f_frame, &s->f_damp};
     for (size_t i = 0; i < sizeof(arrs) / sizeof(arrs[0]); ++i) {
         *arrs[i] = (double*)calloc((size_t)N, sizeof(double));
     }
     /* Generator(initstate = seed + arange(N), initseq = 0), Line1d.h:148-155; Line2d.h:28-34 */
+    OQ_PARALLEL_FOR
     for (int64_t p = 0; p < N; ++p) {
         pcg_seed(seed + (uint64_t)p, 0u, &s->g0[p], &s->inc[p]);
         seq_fill(s, p, 0, nchunk, s->data + p * nchunk);
@@ -1022,32 +1064,45 @@ int oq_time_step(oq_system* s)
     double dt = s->dt, hdt = 0.5 * dt, hdt2 = 0.5 * dt * dt;
     s->inc_n++;
     updated_inc(s);
-    memcpy(s->v_n, s->v, sizeof(double) * (size_t)N);
-    memcpy(s->a_n, s->a, sizeof(double) * (size_t)N);
+    OQ_PARALLEL_FOR
+    for (int64_t p = 0; p < N; ++p) {
+        s->v_n[p] = s->v[p];
+        s->a_n[p] = s->a[p];
+    }
+    OQ_PARALLEL_FOR
     for (int64_t p = 0; p < N; ++p) {
         s->u[p] = s->u[p] + dt * s->v[p] + hdt2 * s->a[p];
     }
     updated_u(s);
+    OQ_PARALLEL_FOR
     for (int64_t p = 0; p < N; ++p) {
         s->v[p] = s->v_n[p] + dt * s->a_n[p];
     }
     updated_v(s);
+    OQ_PARALLEL_FOR
     for (int64_t p = 0; p < N; ++p) {
         s->a[p] = s->f[p] * s->inv_m;
     }
     for (int rep = 0; rep < 2; ++rep) {
+        OQ_PARALLEL_FOR
         for (int64_t p = 0; p < N; ++p) {
             s->v[p] = s->v_n[p] + hdt * (s->a_n[p] + s->a[p]);
         }
         updated_v(s);
+        OQ_PARALLEL_FOR
         for (int64_t p = 0; p < N; ++p) {
             s->a[p] = s->f[p] * s->inv_m;
         }
     }
+    int nan = 0;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) reduction(| : nan)
+#endif
     for (int64_t p = 0; p < N; ++p) {
-        if (isnan(s->u[p])) {
-            return fail(s, OQ_ERR_NAN, "NaN entries found");
-        }
+        nan |= isnan(s->u[p]) ? 1 : 0;
+    }
+    if (nan) {
+        return fail(s, OQ_ERR_NAN, "NaN entries found");
     }
     return OQ_OK;
 }

@@ -21,6 +21,7 @@ import numpy as np
 HERE = pathlib.Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 LIB = BUILD / "libfqsb_oracle.so"
+LIB_MT = BUILD / "libfqsb_oracle_mt.so"  # OpenMP build: per-particle loops over the host cores
 SOURCES = [HERE / "fqsb_oracle.c", HERE / "fqsb_oracle.h", HERE.parent / "frictionqpotspringblock_gb300" / "csrc" / "fq_math.h"]
 
 CUSPY, SEMISMOOTH, SMOOTH = 0, 1, 2
@@ -41,29 +42,29 @@ F_U, F_V, F_A, F_F, F_POT, F_INT, F_FRAME, F_DAMP = range(8)
 S_U_FRAME, S_T, S_TEMPERATURE, S_RESIDUAL, S_MEAN_F_FRAME = range(5)
 
 
-def build(force: bool = False) -> pathlib.Path:
-    """Compile the oracle with gcc (no FMA contraction, no fast-math)."""
+def build(force: bool = False, threads: bool = False) -> pathlib.Path:
+    """Compile the oracle with gcc (no FMA contraction, no fast-math); threads=True builds the OpenMP
+    variant, whose per-particle loops run over the host cores with bit-identical results."""
     BUILD.mkdir(exist_ok=True)
+    target = LIB_MT if threads else LIB
     newest = max(p.stat().st_mtime for p in SOURCES)
-    if force or not LIB.exists() or LIB.stat().st_mtime < newest:
-        tmp = BUILD / f"libfqsb_oracle.{os.getpid()}.so"
+    if force or not target.exists() or target.stat().st_mtime < newest:
+        tmp = BUILD / f"{target.stem}.{os.getpid()}.so"
         cmd = [
             "gcc", "-std=gnu11", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
-            "-o", str(tmp), str(HERE / "fqsb_oracle.c"), "-lm",
+            *(["-fopenmp"] if threads else []), "-o", str(tmp), str(HERE / "fqsb_oracle.c"), "-lm",
         ]
         subprocess.run(cmd, check=True)
-        os.replace(tmp, LIB)
-    return LIB
+        os.replace(tmp, target)
+    return target
 
 
-_lib = None
+_libs = {}
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        build()
-        L = ctypes.CDLL(str(LIB))
+def lib(threads: bool = False):
+    if threads not in _libs:
+        L = ctypes.CDLL(str(build(threads=threads)))
         P = ctypes.c_void_p
         d, i64, u64, i32 = ctypes.c_double, ctypes.c_int64, ctypes.c_uint64, ctypes.c_int
         pd = ctypes.POINTER(ctypes.c_double)
@@ -118,8 +119,8 @@ def lib():
         L.oq_event_driven_step.argtypes = [P, d, i32, i32, pd]
         L.oq_trigger.argtypes = [P, i64, d, i32]
         L.oq_advance_to_fixed_force.argtypes = [P, d, i32]
-        _lib = L
-    return _lib
+        _libs[threads] = L
+    return _libs[threads]
 
 
 def _ptr(a: np.ndarray):
@@ -172,7 +173,7 @@ class _Chunk:
         c = np.empty(s.size, np.int64)
         left = np.empty(s.size)
         right = np.empty(s.size)
-        lib().oq_get_index(s._h, _ptr(g), _ptr(c), _ptr(left), _ptr(right))
+        self._s._L.oq_get_index(s._h, _ptr(g), _ptr(c), _ptr(left), _ptr(right))
         shape = s.shape
         return g.reshape(shape), c.reshape(shape), left.reshape(shape), right.reshape(shape)
 
@@ -196,21 +197,21 @@ class _Chunk:
     def data(self):
         s = self._s
         out = np.empty((s.size, s.nchunk))
-        lib().oq_chunk_data(s._h, _ptr(out), None)
+        self._s._L.oq_chunk_data(s._h, _ptr(out), None)
         return out.reshape(tuple(s.shape) + (s.nchunk,))
 
     @property
     def start(self):
         s = self._s
         out = np.empty(s.size, np.int64)
-        lib().oq_chunk_data(s._h, None, _ptr(out))
+        self._s._L.oq_chunk_data(s._h, None, _ptr(out))
         return out.reshape(s.shape)
 
     def state_at(self, index):
         s = self._s
         idx = np.ascontiguousarray(np.broadcast_to(index, s.shape), dtype=np.int64).ravel()
         out = np.empty(s.size, np.uint64)
-        lib().oq_chunk_state_at(s._h, _ptr(idx), _ptr(out))
+        self._s._L.oq_chunk_state_at(s._h, _ptr(idx), _ptr(out))
         return out.reshape(s.shape)
 
     def restore(self, state, value, index):
@@ -218,7 +219,7 @@ class _Chunk:
         st = np.ascontiguousarray(state, dtype=np.uint64).ravel()
         val = np.ascontiguousarray(value, dtype=np.float64).ravel()
         idx = np.ascontiguousarray(index, dtype=np.int64).ravel()
-        lib().oq_chunk_restore(s._h, _ptr(st), _ptr(val), _ptr(idx))
+        self._s._L.oq_chunk_restore(s._h, _ptr(st), _ptr(val), _ptr(idx))
 
 
 class System:
@@ -226,7 +227,7 @@ class System:
 
     def __init__(self, potential, interactions, shape, m, eta, mu, k_interactions, k_frame, dt, seed,
                  distribution, parameters, offset=-100.0, nchunk=5000, kappa=0.0, offset_per_particle=None,
-                 sum_mode=SUM_PAIRWISE, math_mode=MATH_PORTABLE, interaction_parameters=None):
+                 sum_mode=SUM_PAIRWISE, math_mode=MATH_PORTABLE, interaction_parameters=None, threads=False):
         shape = [int(i) for i in shape]
         rows, cols = (1, shape[0]) if len(shape) == 1 else (shape[0], shape[1])
         self.shape = shape
@@ -237,7 +238,8 @@ class System:
         if offset_per_particle is not None:
             self._offp = np.ascontiguousarray(offset_per_particle, dtype=np.float64).ravel()
             offp = self._offp.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
-        h = lib().oq_create(potential, interactions, rows, cols, m, eta, mu, kappa, k_interactions, k_frame, dt,
+        self._L = lib(threads)
+        h = self._L.oq_create(potential, interactions, rows, cols, m, eta, mu, kappa, k_interactions, k_frame, dt,
                             int(seed), DISTRIBUTIONS[distribution], par, len(parameters), offset, offp, nchunk,
                             sum_mode, math_mode)
         if not h:
@@ -245,27 +247,27 @@ class System:
         self._h = h
         if interaction_parameters is not None:
             a, b = (float(x) for x in interaction_parameters)
-            self._check(lib().oq_set_interaction_parameters(h, a, b))
+            self._check(self._L.oq_set_interaction_parameters(h, a, b))
         self.dt, self.mu, self.eta, self.m, self.k_frame = dt, mu, eta, m, k_frame
         self.chunk = _Chunk(self)
 
     def __del__(self):
         if getattr(self, "_h", None):
-            lib().oq_destroy(self._h)
+            self._L.oq_destroy(self._h)
             self._h = None
 
     def _check(self, rc):
         if rc != 0:
-            raise OracleError(lib().oq_last_error(self._h).decode())
+            raise OracleError(self._L.oq_last_error(self._h).decode())
 
     def _get(self, field):
         out = np.empty(self.size)
-        lib().oq_get(self._h, field, _ptr(out))
+        self._L.oq_get(self._h, field, _ptr(out))
         return out.reshape(self.shape)
 
     def _set(self, field, value):
         arr = np.ascontiguousarray(np.broadcast_to(value, self.shape), dtype=np.float64)
-        self._check(lib().oq_set(self._h, field, _ptr(arr)))
+        self._check(self._L.oq_set(self._h, field, _ptr(arr)))
 
     u = property(lambda s: s._get(F_U), lambda s, x: s._set(F_U, x))
     v = property(lambda s: s._get(F_V), lambda s, x: s._set(F_V, x))
@@ -275,102 +277,102 @@ class System:
     f_interactions = property(lambda s: s._get(F_INT))
     f_frame = property(lambda s: s._get(F_FRAME))
     f_damping = property(lambda s: s._get(F_DAMP))
-    temperature = property(lambda s: lib().oq_get_scalar(s._h, S_TEMPERATURE))
-    residual = property(lambda s: lib().oq_get_scalar(s._h, S_RESIDUAL))
-    mean_f_frame = property(lambda s: lib().oq_get_scalar(s._h, S_MEAN_F_FRAME))
-    quasistaticActivityFirst = property(lambda s: lib().oq_quasistatic_first(s._h))
-    quasistaticActivityLast = property(lambda s: lib().oq_quasistatic_last(s._h))
+    temperature = property(lambda s: self._L.oq_get_scalar(s._h, S_TEMPERATURE))
+    residual = property(lambda s: self._L.oq_get_scalar(s._h, S_RESIDUAL))
+    mean_f_frame = property(lambda s: self._L.oq_get_scalar(s._h, S_MEAN_F_FRAME))
+    quasistaticActivityFirst = property(lambda s: self._L.oq_quasistatic_first(s._h))
+    quasistaticActivityLast = property(lambda s: self._L.oq_quasistatic_last(s._h))
 
     @property
     def u_frame(self):
-        return lib().oq_get_scalar(self._h, S_U_FRAME)
+        return self._L.oq_get_scalar(self._h, S_U_FRAME)
 
     @u_frame.setter
     def u_frame(self, value):
-        lib().oq_set_u_frame(self._h, float(value))
+        self._L.oq_set_u_frame(self._h, float(value))
 
     @property
     def inc(self):
-        return lib().oq_get_inc(self._h)
+        return self._L.oq_get_inc(self._h)
 
     @inc.setter
     def inc(self, value):
-        lib().oq_set_inc(self._h, int(value))
+        self._L.oq_set_inc(self._h, int(value))
 
     @property
     def t(self):
-        return lib().oq_get_scalar(self._h, S_T)
+        return self._L.oq_get_scalar(self._h, S_T)
 
     @t.setter
     def t(self, value):
-        lib().oq_set_t(self._h, float(value))
+        self._L.oq_set_t(self._h, float(value))
 
     @property
     def i(self):
         return self.chunk.index_at_align
 
     def refresh(self):
-        lib().oq_refresh(self._h)
+        self._L.oq_refresh(self._h)
 
     def quench(self):
-        lib().oq_quench(self._h)
+        self._L.oq_quench(self._h)
 
     def timeStep(self):
-        self._check(lib().oq_time_step(self._h))
+        self._check(self._L.oq_time_step(self._h))
 
     def timeSteps(self, n):
-        self._check(lib().oq_time_steps(self._h, int(n)))
+        self._check(self._L.oq_time_steps(self._h, int(n)))
 
     def flowSteps(self, n, v_frame):
-        self._check(lib().oq_flow_steps(self._h, int(n), float(v_frame)))
+        self._check(self._L.oq_flow_steps(self._h, int(n), float(v_frame)))
 
     def timeStepsUntilEvent(self, tol=1e-5, niter_tol=10, max_iter=int(1e9)):
         r = ctypes.c_uint64()
-        self._check(lib().oq_time_steps_until_event(self._h, tol, niter_tol, max_iter, ctypes.byref(r)))
+        self._check(self._L.oq_time_steps_until_event(self._h, tol, niter_tol, max_iter, ctypes.byref(r)))
         return r.value
 
     def minimise(self, tol=1e-5, niter_tol=10, max_iter=int(1e9), time_activity=False, max_iter_is_error=True):
         r = ctypes.c_uint64()
-        self._check(lib().oq_minimise(self._h, tol, niter_tol, int(max_iter), int(time_activity),
+        self._check(self._L.oq_minimise(self._h, tol, niter_tol, int(max_iter), int(time_activity),
                                       int(max_iter_is_error), ctypes.byref(r)))
         return r.value
 
     @property
     def f_thermal(self):
         out = np.empty(self.size)
-        self._check(lib().oq_get_thermal(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        self._check(self._L.oq_get_thermal(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
         return out.reshape(self.shape)
 
     @f_thermal.setter
     def f_thermal(self, value):
         a = np.ascontiguousarray(np.broadcast_to(value, self.shape), dtype=np.float64).ravel()
-        self._check(lib().oq_thermal_set(self._h, None, a.ctypes.data, None))
+        self._check(self._L.oq_thermal_set(self._h, None, a.ctypes.data, None))
 
     @property
     def thermal_state(self):
         out = ctypes.c_uint64()
-        self._check(lib().oq_thermal_get(self._h, ctypes.addressof(out), None, None))
+        self._check(self._L.oq_thermal_get(self._h, ctypes.addressof(out), None, None))
         return out.value
 
     @thermal_state.setter
     def thermal_state(self, value):
         st = ctypes.c_uint64(int(value))
-        self._check(lib().oq_thermal_set(self._h, ctypes.addressof(st), None, None))
+        self._check(self._L.oq_thermal_set(self._h, ctypes.addressof(st), None, None))
 
     @property
     def thermal_next(self):
         out = np.empty(self.size, np.int64)
-        self._check(lib().oq_thermal_get(self._h, None, None, out.ctypes.data))
+        self._check(self._L.oq_thermal_get(self._h, None, None, out.ctypes.data))
         return out.reshape(self.shape)
 
     @thermal_next.setter
     def thermal_next(self, value):
         a = np.ascontiguousarray(np.broadcast_to(value, self.shape), dtype=np.int64).ravel()
-        self._check(lib().oq_thermal_set(self._h, None, None, a.ctypes.data))
+        self._check(self._L.oq_thermal_set(self._h, None, None, a.ctypes.data))
 
     def minimise_nopassing(self, tol=1e-5, niter_tol=10, max_iter=int(1e9), max_iter_is_error=True):
         r = ctypes.c_uint64()
-        self._check(lib().oq_minimise_nopassing(self._h, tol, niter_tol, int(max_iter), int(max_iter_is_error),
+        self._check(self._L.oq_minimise_nopassing(self._h, tol, niter_tol, int(max_iter), int(max_iter_is_error),
                                                 ctypes.byref(r)))
         return r.value
 
@@ -378,30 +380,30 @@ class System:
                           time_activity=True, max_iter_is_error=True):
         idx = np.ascontiguousarray(i_n, dtype=np.int64).ravel()
         r = ctypes.c_uint64()
-        self._check(lib().oq_minimise_truncate(self._h, _ptr(idx), A_truncate, S_truncate, tol, niter_tol,
+        self._check(self._L.oq_minimise_truncate(self._h, _ptr(idx), A_truncate, S_truncate, tol, niter_tol,
                                                int(max_iter), int(time_activity), int(max_iter_is_error),
                                                ctypes.byref(r)))
         return r.value
 
     def maxUniformDisplacement(self, direction=1):
         r = ctypes.c_double()
-        self._check(lib().oq_max_uniform_displacement(self._h, direction, ctypes.byref(r)))
+        self._check(self._L.oq_max_uniform_displacement(self._h, direction, ctypes.byref(r)))
         return r.value
 
     def eventDrivenStep(self, eps, kick, direction=1):
         r = ctypes.c_double()
-        self._check(lib().oq_event_driven_step(self._h, eps, int(kick), direction, ctypes.byref(r)))
+        self._check(self._L.oq_event_driven_step(self._h, eps, int(kick), direction, ctypes.byref(r)))
         return r.value
 
     def trigger(self, p, eps, direction=1):
-        self._check(lib().oq_trigger(self._h, int(p), eps, direction))
+        self._check(self._L.oq_trigger(self._h, int(p), eps, direction))
 
     def advanceToFixedForce(self, f_frame, allow_plastic=False):
-        self._check(lib().oq_advance_to_fixed_force(self._h, f_frame, int(allow_plastic)))
+        self._check(self._L.oq_advance_to_fixed_force(self._h, f_frame, int(allow_plastic)))
 
     def yield_sequence(self, p, k0, count):
         out = np.empty(count)
-        self._check(lib().oq_yield_sequence(self._h, p, k0, count, _ptr(out)))
+        self._check(self._L.oq_yield_sequence(self._h, p, k0, count, _ptr(out)))
         return out
 
 
@@ -487,7 +489,7 @@ def attach_random_forcing(s, mean, stddev, seed_forcing, dinc_init, dinc):
     s._th_next = np.ascontiguousarray(np.broadcast_to(dinc_init, (n,)), dtype=np.int64)
     s._th_dinc = np.ascontiguousarray(np.broadcast_to(dinc, (n,)), dtype=np.int64)
     state, inc = pcg32_seed(int(seed_forcing))
-    s._check(lib().oq_set_thermal(s._h, float(mean), float(stddev), state, inc, s._th_next.ctypes.data,
+    s._check(s._L.oq_set_thermal(s._h, float(mean), float(stddev), state, inc, s._th_next.ctypes.data,
                                   s._th_dinc.ctypes.data, 0))
     return s
 

@@ -72,7 +72,9 @@ def signatures(src):
 
 
 def main():
-    ref = pathlib.Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) < 2:
+        sys.exit(f"usage: python {pathlib.Path(__file__).name} <root of the reference project>")
+    ref = pathlib.Path(sys.argv[1])
     src = (ref / "python" / "main.cpp").read_text()
     classes = {}
     binders = {}

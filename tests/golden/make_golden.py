@@ -41,7 +41,9 @@ def read(path: pathlib.Path, n: int, first: str):
 
 
 def main():
-    ref = pathlib.Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) < 2:
+        sys.exit(f"usage: python {pathlib.Path(__file__).name} <root of the reference project>")
+    ref = pathlib.Path(sys.argv[1])
     out = pathlib.Path(__file__).parent
     for stem, (n, first) in FILES.items():
         frame, f_frame, S = read(ref / "examples" / (stem + ".h5"), n, first)

@@ -1,6 +1,8 @@
 """The committed fixtures are what their committed scripts make from the reference tree: the golden
 trajectories (tests/golden/make_golden.py, from examples/*.h5) and the API names
-(tests/golden/make_api_names.py, from python/main.cpp).  Skipped where the reference tree is absent."""
+(tests/golden/make_api_names.py, from python/main.cpp).  Runs when FQSB_REFERENCE_ROOT names the root of the
+reference project (e.g. FQSB_REFERENCE_ROOT=<path> python -m pytest tests/test_fixtures_regenerate.py), else
+skipped."""
 
 import importlib.util
 import json
@@ -12,9 +14,10 @@ import numpy as np
 import pytest
 
 GOLDEN = pathlib.Path(__file__).parent / "golden"
-REF = pathlib.Path(os.environ.get("FQSB_REFERENCE_ROOT", "/root/reference"))
+REF = pathlib.Path(os.environ.get("FQSB_REFERENCE_ROOT", "")) if os.environ.get("FQSB_REFERENCE_ROOT") else None
 
-pytestmark = pytest.mark.skipif(not (REF / "python" / "main.cpp").exists(), reason="reference tree not present")
+pytestmark = pytest.mark.skipif(REF is None or not (REF / "python" / "main.cpp").exists(),
+                                reason="FQSB_REFERENCE_ROOT does not name the reference tree")
 
 
 def _load(name):

@@ -165,3 +165,22 @@ def test_adjoint_leaves_final_state():
     system.adjoint_backward()
     assert np.array_equal(system.u, uT)
     assert system.u_frame == sched[-1]
+
+
+def test_autograd_cuda_tensors():
+    """CUDA tensors on the system's device go through the device entry points (no host round trip of
+    u0, v0 or their gradients) and give the same loss and gradients, bit for bit, as host tensors."""
+    system = make("Smooth")
+    u0, v0, sched, params = inputs(4)
+    out = []
+    for dev in ("cpu", "cuda:0"):
+        tu0 = torch.tensor(u0, device=dev, requires_grad=True)
+        tv0 = torch.tensor(v0, device=dev, requires_grad=True)
+        tsch = torch.tensor(sched, device=dev, requires_grad=True)
+        tpar = torch.tensor(params, device=dev, requires_grad=True)
+        loss = trajectory_loss(system, tu0, tv0, tsch, tpar, K=K, last=LAST)
+        loss.backward()
+        assert tu0.grad.device == tu0.device and tv0.grad.device == tv0.device
+        out.append([loss.detach().cpu()] + [x.grad.detach().cpu() for x in (tu0, tv0, tsch, tpar)])
+    for a, b in zip(*out):
+        assert torch.equal(a, b)

@@ -18,14 +18,16 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def test_residual_noalloc_matches_handle_residual():
+@pytest.mark.parametrize("n", [300001, 100000, 1000])
+def test_residual_noalloc_matches_handle_residual(n):
+    """n = 300001 fills more than 256 tiles of 1024 entries (the final pass sums the tile partials in a
+    loop); 100000 and 1000 fit one CTA's tree of at most 256 partials."""
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("needs a GPU")
     from frictionqpotspringblock_gb300 import Line1d, _capi
 
     lib = _capi.lib()
-    n = 300001  # not a multiple of the 1024-entry tiles
     system = Line1d.System_Cuspy_Laplace(m=1.0, eta=0.1, mu=1.0, k_interactions=1.0, k_frame=1.0 / n, dt=0.1,
                                          shape=[n], seed=7, distribution="weibull", parameters=[2.0, 1.0, 1e-5],
                                          offset=-100.0, nchunk=200)
