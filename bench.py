@@ -11,14 +11,24 @@ seed 1), v = 0.  The frame is ramped by 1e-4 per time step
 One bench step = flowSteps(1000): 1000 fused time steps over all particles,
 so --steps 10 covers the configuration's 10^4 steps.  The metric is
 particle-steps/s (FP64).  After the timed steps the +0.5 jump and minimise are
-run once and their wall time is reported (minimise_s).
+run once and their wall time is reported (minimise).
 
 `value` times the device-resident steps (state already in HBM); `e2e` times
 the same steps through the public API with host buffers: each step copies u
 and v from pinned host memory into the system, runs flowSteps(1000) and reads
-u back.  `--impl reference` times the CPU reference path instead (the CPU
-oracle, a loop-per-statement restatement of the reference, on the host
-cores), on bounded samples of the same workload.
+u back.  `--impl reference` times the CPU reference path instead: the oracle
+(the reference's loop-per-statement integrator restated in C, libm, built with
+OpenMP so its per-particle loops run over all host cores with bit-identical
+results) on the same N = 2^22 ring, seeds and initial state, each bench step a
+bounded number of flowSteps time steps.
+
+`forms` times the other configurations (each records an error instead of
+raising): small_system (N = 1024 quasistatic protocol), line2d (2048 x 2048
+grid), batched (4096 uneven realisations), adjoint (N = 65536, T = 5000
+differentiation with finite-difference checks) and next_rows (the further
+interactions, the no-passing minimiser, the thermal forcing).  By default the
+long protocols run shortened (stated in each entry); --full runs them at their
+configured sizes; --forms selects a subset.
 
 Multi-GPU (torchrun): the plain path does not shard (one system fits one GPU),
 so every rank runs an independent replica (weak scaling); value = sum of the
@@ -31,6 +41,7 @@ import argparse
 import json
 import os
 import pathlib
+import re
 import statistics
 import subprocess
 import sys
@@ -49,18 +60,17 @@ PAR = dict(m=1.0, eta=0.1, mu=1.0, k_interactions=1.0, dt=0.1, seed=1, distribut
            parameters=[2.0, 1.0, 1e-5], offset=-100.0, nchunk=2000)
 V_FRAME = 1e-3  # u_frame += v_frame * dt = 1e-4 per step
 BYTES_PER_PARTICLE_STEP = 64  # read+write u, v, a (48 B) + read the current well {y_left, y_right} (16 B)
-# DRAM bytes per particle per step of the step kernel from one ncu capture (N = 2^21, dram__bytes_read.sum
-# + dram__bytes_write.sum = 147.49 MB per launch; profiles/k_step_line_cuspy_laplace1d_N4M.md), scaled by N
-TRAFFIC_BYTES_PER_PARTICLE_STEP = 147.49e6 / 2097152
 FP64_OPS_PER_PARTICLE_STEP = 24  # binary64 add/mul of the exact-order step; compares and 2^k scalings are integer work
 # of those, the step kernel issues these on the fp64 pipe; the rest (the 8 multiplications and the 2 additions of
 # the position update) run bit-identically on the integer pipes (csrc/fq_soft64.h)
 FP64_PIPE_OPS_PER_PARTICLE_STEP = 14
+STEP_PROFILE = ROOT / "profiles" / "k_step_line_cuspy_laplace1d_N4M.md"
+FORMS = ("small_system", "line2d", "batched", "adjoint", "next_rows")
 
 
-def workload(n):
+def workload(n, inner=INNER):
     return (f"Line1d System_Cuspy_Laplace N={n} ring, m=1 eta=0.1 mu=1 k=1 k_frame=1/N dt=0.1, "
-            f"weibull(2,1)+1e-5 nchunk=2000 seed=1, u0~N(0,0.1^2); step = flowSteps({INNER}, v_frame=1e-3) "
+            f"weibull(2,1)+1e-5 nchunk=2000 seed=1, u0~N(0,0.1^2); step = flowSteps({inner}, v_frame=1e-3) "
             f"(u_frame +1e-4 per time step); then u_frame += 0.5 and minimise(tol=1e-5)")
 
 
@@ -70,6 +80,16 @@ def peaks():
         d = json.loads(p.read_text())
         return float(d.get("hbm_gbs", 6800.0)), "measured"
     return 6800.0, "fallback"
+
+
+def profile_figures(path=STEP_PROFILE):
+    """`name = number` lines of a committed profile summary (the ncu figures the roofline uses)."""
+    out = {}
+    for line in path.read_text().splitlines():
+        m = re.fullmatch(r"\s+([a-z_]+) = ([0-9.eE+-]+)", line)
+        if m:
+            out[m.group(1)] = float(m.group(2))
+    return out
 
 
 class ClockSampler:
@@ -121,11 +141,119 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def bench_batched(fqsb, n_inst=512, n_loop=32):
-    """Batched form on the first n_inst realisations of the 4096-realisation size list (log-uniform in
-    [256, 65536] from pcg32 seed 3; seed 1000+j; k_frame = 1/N_j; Weibull(2,1)+1e-5; 1000-position
-    chunk), one quasistatic cycle each, with the tile shape the autotuner picks; against looping the
-    plain path over the first n_loop."""
+def _guard(fn, *a, **kw):
+    """A form's failure is recorded in its entry, not raised: the bench line must still be printed."""
+    try:
+        return fn(*a, **kw)
+    except Exception as e:  # noqa: BLE001
+        return {"error": f"{type(e).__name__}: {e}"}
+
+
+def _sync_seconds(t0):
+    import torch
+
+    torch.cuda.synchronize()
+    return time.perf_counter() - t0
+
+
+# ------------------------------------------------------------------------------------------ forms
+
+def bench_small(fqsb, full=False, cycles=100, cpu_cycles=10):
+    """Small system: Line1d System_Cuspy_Laplace N = 1024, m = 1, eta = 0.1, mu = 1, k = 1,
+    k_frame = 1/1024, dt = 0.1, Weibull(2,1)+1e-5 seed 0, 1000-position chunk shifted per particle so
+    that u = 0 is the centre of well 500; from u = v = 0, 100 cycles of eventDrivenStep(1e-5,
+    kick=False), eventDrivenStep(1e-5, kick=True), minimise(tol=1e-5, max_iter=1e6).  The CPU oracle
+    (the reference restated: libm, sequential sums, one core) runs the first `cpu_cycles` cycles of the
+    same protocol; the GPU is timed over the same first cycles and over all 100."""
+    N = 1024
+    par = dict(m=1.0, eta=0.1, mu=1.0, k_interactions=1.0, k_frame=1.0 / N, dt=0.1, shape=[N], seed=0,
+               distribution="weibull", parameters=[2.0, 1.0, 1e-5], nchunk=1000)
+    plain = fqsb.Line1d.System_Cuspy_Laplace(offset=0.0, **par)
+    raw, start = plain.chunk.data, plain.chunk.start  # the window moved so that u = 0 lies inside it
+    rows = np.arange(N)
+    offp = -0.5 * (raw[rows, 500 - start] + raw[rows, 501 - start])
+    del plain
+
+    def run(s, n):
+        inc0 = s.inc
+        t0 = time.perf_counter()
+        for _ in range(n):
+            s.eventDrivenStep(1e-5, False)
+            s.eventDrivenStep(1e-5, True)
+            s.minimise(max_iter=1000000)
+        return time.perf_counter() - t0, s.inc - inc0
+
+    s = fqsb.Line1d.System_Cuspy_Laplace(offset=0.0, offset_per_particle=offp, **par)
+    assert np.all(s.chunk.index_at_align == 500)
+    t_first, steps_first = run(s, cpu_cycles)
+    t_rest, steps_rest = run(s, cycles - cpu_cycles)
+    t, steps = t_first + t_rest, steps_first + steps_rest
+    out = {"particles": N, "cycles": cycles, "seconds": t, "seconds_per_cycle": t / cycles, "time_steps": steps,
+           "us_per_step": 1e6 * t / steps, "first_cycles": {"cycles": cpu_cycles, "seconds": t_first,
+                                                             "time_steps": steps_first}}
+    if cpu_cycles > 0:
+        from oracle import oracle as O  # the CPU baseline: the reference restated, one core
+
+        r = O.line1d("Cuspy", offset=0.0, offset_per_particle=offp, sum_mode=O.SUM_SEQUENTIAL, math_mode=O.MATH_LIBM,
+                     **par)
+        tc, sc = run(r, cpu_cycles)
+        out["cpu_oracle"] = {"cycles": cpu_cycles, "cores": 1, "seconds": tc, "time_steps": sc,
+                             "us_per_step": 1e6 * tc / sc}
+        out["speedup_vs_cpu_oracle_same_cycles"] = tc / t_first
+    return out
+
+
+def bench_line2d(fqsb, full=False):
+    """Line2d System_Cuspy_Laplace on a 2048 x 2048 periodic grid: m = 1, eta = 0.2, mu = 1, k = 1,
+    k_frame = 1/2048^2, dt = 0.1, Weibull(2,1)+1e-5 from pcg32 seed 2, 500 yield positions per site;
+    cycles of eventDrivenStep(1e-5, kick=False), eventDrivenStep(1e-5, kick=True), minimise(tol=1e-5)
+    (20 with --full, else 1 warm-up + 2 timed); then a regeneration sweep: u += 600 and back (every
+    site crosses ~680 wells, so every chunk window is regenerated from its pcg32 stream, forward then
+    backward)."""
+    side = 2048
+    n = side * side
+    s = fqsb.Line2d.System_Cuspy_Laplace(m=1.0, eta=0.2, mu=1.0, k_interactions=1.0, k_frame=1.0 / n, dt=0.1,
+                                         shape=[side, side], seed=2, distribution="weibull",
+                                         parameters=[2.0, 1.0, 1e-5], offset=-100.0, nchunk=500)
+    ncycles = 20 if full else 2
+    out = {"shape": [side, side], "cycles": ncycles, "per_cycle": []}
+    if not full:
+        s.eventDrivenStep(1e-5, False)
+        s.eventDrivenStep(1e-5, True)
+        s.minimise()
+    tot_t, tot_steps = 0.0, 0
+    for _ in range(ncycles):
+        inc0 = s.inc
+        t0 = time.perf_counter()
+        s.eventDrivenStep(1e-5, False)
+        s.eventDrivenStep(1e-5, True)
+        t1 = time.perf_counter()
+        ret = s.minimise()
+        t2 = time.perf_counter()
+        steps = s.inc - inc0
+        tot_t += t2 - t0
+        tot_steps += steps
+        out["per_cycle"].append({"event_s": t1 - t0, "minimise_s": t2 - t1, "time_steps": steps, "ret": ret})
+    ps = n * tot_steps / tot_t
+    out.update(seconds=tot_t, time_steps=tot_steps, particle_steps_per_s=ps,
+               hbm_frac_64B=BYTES_PER_PARTICLE_STEP * ps / 1e9 / peaks()[0])
+    u = s.u
+    t0 = time.perf_counter()
+    s.u = u + 600.0
+    t1 = time.perf_counter()
+    s.u = u
+    t2 = time.perf_counter()
+    out["regeneration_sweep"] = {"forward_s": t1 - t0, "backward_s": t2 - t1, "wells_crossed_per_site": "~680"}
+    return out
+
+
+def bench_batched(fqsb, full=False):
+    """Batched form on all 4096 realisations of the size list (N_j log-uniform in [256, 65536] from
+    pcg32 seed 3; pcg32 seed 1000+j; k_frame = 1/N_j; Weibull(2,1)+1e-5; 1000-position chunk, 64 kept),
+    cycles of eventDrivenStep(1e-5, False), eventDrivenStep(1e-5, True), minimise(tol=1e-5) (50 with
+    --full, else 1) with the tile shape the autotuner picks; against the plain path looped over a random
+    sample of the realisations (256 with --full, else 64; seed 5) for the same cycles, scaled to all
+    realisations by their share of the particles."""
     from frictionqpotspringblock_gb300 import autotune as A
     from frictionqpotspringblock_gb300 import batch as B
 
@@ -133,120 +261,110 @@ def bench_batched(fqsb, n_inst=512, n_loop=32):
                parameters=[2.0, 1.0, 1e-5], offset=-100.0)
     sizes = B.log_uniform_sizes(4096, 256, 65536, seed=3)
     seeds = 1000 + np.arange(4096)
-    out = {}
+    ncycles = 50 if full else 1
+    nloop = 256 if full else 64
+    out = {"realisations": 4096, "particles": int(sizes.sum()), "cycles": ncycles}
 
-    # tile shape (threads x particles per thread) from the autotuner: timed on a sample of the batch
     def make(sz, threads, ppt):
         return B.Line1d_System_Cuspy_Laplace(sz, 1000 + np.arange(len(sz)), 1.0 / sz, nchunk=1000, window=64,
                                              threads=threads, ppt=ppt, **par)
 
     t0 = time.perf_counter()
-    threads, ppt = A.choose_tile(sizes[:n_inst], make, use_cache=False)
+    threads, ppt = A.choose_tile(sizes[:512], make, use_cache=False)
     out.update(tile=[int(threads), int(ppt)], autotune_seconds=time.perf_counter() - t0)
-    b = B.Line1d_System_Cuspy_Laplace(sizes[:n_inst], seeds[:n_inst], 1.0 / sizes[:n_inst], nchunk=1000, window=64,
-                                      threads=threads, ppt=ppt, **par)
+    b = B.Line1d_System_Cuspy_Laplace(sizes, seeds, 1.0 / sizes, nchunk=1000, window=64, threads=threads, ppt=ppt,
+                                      **par)
     t0 = time.perf_counter()
-    r = b.quasistatic(1, 1e-5)
+    r = b.quasistatic(ncycles, 1e-5)
     t = time.perf_counter() - t0
-    ps = int((r["inc"][:, -1] * sizes[:n_inst]).sum())
-    out.update(realisations=n_inst, particles=int(sizes[:n_inst].sum()), seconds=t, particle_steps=ps, value=ps / t)
+    ps = int((r["inc"][:, -1] * sizes).sum())
+    out.update(seconds=t, particle_steps=ps, value=ps / t, converged=int(np.sum(r["status"] == 0)))
     del b
-    b = B.Line1d_System_Cuspy_Laplace(sizes[:n_loop], seeds[:n_loop], 1.0 / sizes[:n_loop], nchunk=1000, window=64,
-                                      threads=threads, ppt=ppt, **par)
-    t0 = time.perf_counter()
-    r = b.quasistatic(1, 1e-5)
-    tb = time.perf_counter() - t0
-    del b
-    tp = 0.0
-    for j in range(n_loop):
+    pick = np.sort(np.random.default_rng(5).choice(4096, nloop, replace=False))
+    tp, pps = 0.0, 0
+    for j in pick:
         s = fqsb.Line1d.System_Cuspy_Laplace(k_frame=1.0 / float(sizes[j]), shape=[int(sizes[j])], seed=int(seeds[j]),
                                              nchunk=1000, **par)
         t0 = time.perf_counter()
-        s.eventDrivenStep(1e-5, False)
-        s.eventDrivenStep(1e-5, True)
-        s.minimise()
+        for _ in range(ncycles):
+            s.eventDrivenStep(1e-5, False)
+            s.eventDrivenStep(1e-5, True)
+            s.minimise()
         tp += time.perf_counter() - t0
+        pps += s.inc * int(sizes[j])
         del s
-    out.update(loop_realisations=n_loop, loop_plain_seconds=tp, loop_batched_seconds=tb, speedup_vs_plain_loop=tp / tb)
+    share = float(sizes[pick].sum()) / float(sizes.sum())
+    out["plain_loop"] = {"sample": int(nloop), "sample_seed": 5, "seconds": tp, "particle_steps": pps,
+                         "particle_share": share, "scaled_seconds": tp / share}
+    out["speedup_vs_plain_loop"] = (tp / share) / t
     return out
 
 
-def bench_adjoint(fqsb, N=65536, T=5000, K=100, last=500):
+def bench_adjoint(fqsb, full=False, N=65536, T=5000, K=100, last=500):
     """Adjoint of the differentiation workload: Line1d System_Smooth_Laplace, N = 65536, k_frame = 1/N,
     Weibull(2,1)+1e-5 seed 4, u0 = v0 = 0, u_frame(t) = 1e-3 t + 0.05 sin(2 pi t / 500), T = 5000,
-    checkpoints every 100 steps; forward vs forward + backward wall time."""
+    checkpoints every 100 steps; forward vs forward + backward wall time.  Gradient check: central
+    finite differences (h = 1e-6) of the forward's loss along mu, k_interactions and eta, and along one
+    random direction (seed 9, unit max-norm) of u0, v0 and the schedule each; relative error against the
+    adjoint's directional derivative.  `fd_noise` is the finite difference's own resolution: the loss
+    rounded at 4 ulp, divided by h."""
     s = fqsb.Line1d.System_Smooth_Laplace(m=1.0, eta=0.1, mu=1.0, k_interactions=1.0, k_frame=1.0 / N, dt=0.1,
                                           shape=[N], seed=4, distribution="weibull", parameters=[2.0, 1.0, 1e-5],
                                           offset=-100.0, nchunk=1000)
     t = np.arange(T)
     sched = 1e-3 * t + 0.05 * np.sin(2 * np.pi * t / 500)
     zero = np.zeros(N)
+    params = np.array([1.0, 1.0, 0.1])
+
+    def loss(u0=zero, v0=zero, sc=sched, p=params):
+        s.set_parameters(*p)
+        s.u, s.v, s.a = u0, v0, zero
+        return s.adjoint_forward(sc, K=K, last=last)
+
     for _ in range(2):
-        s.u, s.v, s.a = zero, zero, zero
-        s.adjoint_forward(sched, K=K, last=last)
+        loss()
+    s.set_parameters(*params)
     s.u, s.v, s.a = zero, zero, zero
     t0 = time.perf_counter()
-    loss = s.adjoint_forward(sched, K=K, last=last)
+    L0 = s.adjoint_forward(sched, K=K, last=last)
     tf = time.perf_counter() - t0
     t0 = time.perf_counter()
     gu, gv, gs, gp = s.adjoint_backward()
     tb = time.perf_counter() - t0
-    return {"particles": N, "steps": T, "checkpoint_every": K, "loss": loss, "forward_s": tf, "backward_s": tb,
-            "backward_over_forward": tb / tf, "total_over_forward": (tf + tb) / tf,
-            "grad_norms": {"u0": float(np.linalg.norm(gu)), "schedule": float(np.linalg.norm(gs)),
-                           "params": [float(x) for x in gp]}}
-
-
-def bench_small(fqsb, cycles=20, cpu_cycles=3):
-    """Small system: Line1d System_Cuspy_Laplace N = 1024, k_frame = 1/1024, Weibull(2,1)+1e-5 seed 0,
-    1000-position chunk shifted per particle so that u = 0 is the centre of well 500; cycles of
-    eventDrivenStep(1e-5, kick=False), eventDrivenStep(1e-5, kick=True), minimise(tol=1e-5)."""
-    par = dict(m=1.0, eta=0.1, mu=1.0, k_interactions=1.0, k_frame=1.0 / 1024, dt=0.1, shape=[1024], seed=0,
-               distribution="weibull", parameters=[2.0, 1.0, 1e-5], nchunk=1000)
-    raw = fqsb.Line1d.System_Cuspy_Laplace(offset=0.0, **par).chunk.data
-    offp = -0.5 * (raw[:, 500] + raw[:, 501])
-    s = fqsb.Line1d.System_Cuspy_Laplace(offset=0.0, offset_per_particle=offp, **par)
-    s.eventDrivenStep(1e-5, False)
-    s.eventDrivenStep(1e-5, True)
-    s.minimise(max_iter=1000000)
-    inc0 = s.inc
-    t0 = time.perf_counter()
-    for _ in range(cycles):
-        s.eventDrivenStep(1e-5, False)
-        s.eventDrivenStep(1e-5, True)
-        s.minimise(max_iter=1000000)
-    t = time.perf_counter() - t0
-    out = {"particles": 1024, "cycles": cycles, "seconds_per_cycle": t / cycles,
-           "steps_per_cycle": (s.inc - inc0) / cycles, "us_per_step": 1e6 * t / max(1, s.inc - inc0)}
-    if cpu_cycles > 0:
-        # the same protocol on the CPU oracle (the reference restated: libm, sequential sums), one core
-        from oracle import oracle as O
-
-        r = O.line1d("Cuspy", offset=0.0, offset_per_particle=offp, sum_mode=O.SUM_SEQUENTIAL, math_mode=O.MATH_LIBM,
-                     **par)
-        r.eventDrivenStep(1e-5, False)
-        r.eventDrivenStep(1e-5, True)
-        r.minimise(max_iter=1000000)
-        inc0 = r.inc
-        t0 = time.perf_counter()
-        for _ in range(cpu_cycles):
-            r.eventDrivenStep(1e-5, False)
-            r.eventDrivenStep(1e-5, True)
-            r.minimise(max_iter=1000000)
-        tc = time.perf_counter() - t0
-        out["cpu_oracle"] = {"cycles": cpu_cycles, "cores": 1, "us_per_step": 1e6 * tc / max(1, r.inc - inc0)}
-        out["speedup_vs_cpu_oracle"] = out["cpu_oracle"]["us_per_step"] / out["us_per_step"]
+    out = {"particles": N, "steps": T, "checkpoint_every": K, "loss": L0, "forward_s": tf, "backward_s": tb,
+           "backward_over_forward": tb / tf, "total_over_forward": (tf + tb) / tf}
+    h = 1e-6
+    noise = 4 * np.spacing(abs(L0)) / h
+    checks = {}
+    for i, name in enumerate(["mu", "k_interactions", "eta"]):
+        e = np.zeros(3)
+        e[i] = h
+        fd = (loss(p=params + e) - loss(p=params - e)) / (2 * h)
+        checks[name] = {"adjoint": float(gp[i]), "fd": fd, "rel_err": abs(fd - gp[i]) / abs(gp[i]),
+                        "fd_noise_rel": noise / abs(gp[i])}
+    rng = np.random.default_rng(9)
+    for name, g, x in [("u0", gu, zero), ("v0", gv, zero), ("schedule", gs, sched)]:
+        d = rng.uniform(-1.0, 1.0, x.shape)
+        d /= np.max(np.abs(d))
+        kw_p = {"u0": "u0", "v0": "v0", "schedule": "sc"}[name]
+        fd = (loss(**{kw_p: x + h * d}) - loss(**{kw_p: x - h * d})) / (2 * h)
+        an = float(np.dot(g.ravel(), d.ravel()))
+        checks[name] = {"adjoint": an, "fd": fd, "rel_err": abs(fd - an) / abs(an), "fd_noise_rel": noise / abs(an)}
+    out["gradient_check"] = checks
     return out
 
 
-def bench_next_rows(fqsb, n=2 ** 22, side=2048, n_lr=16384, n_np=2 ** 17, steps=200):
-    """The further interaction types and the no-passing minimiser, each on its own system (Cuspy,
-    Weibull(2,1)+1e-5 seed 2, 200-position chunk, m = 1, eta = 0.1, mu = 1, dt = 0.1, k_frame = 1/N,
-    u ~ N(0, 0.1^2)), timed with the handle's synchronous calls after 20 warm-up steps:
+def bench_next_rows(fqsb, full=False, n=2 ** 22, side=2048, n_lr=16384, n_np=2 ** 17, steps=200):
+    """The further interaction types, the no-passing minimiser and the thermal forcing, each on its own
+    system (Cuspy, Weibull(2,1)+1e-5 seed 2, 200-position chunk, m = 1, eta = 0.1, mu = 1, dt = 0.1,
+    k_frame = 1/N, u ~ N(0, 0.1^2)), timed with the handle's synchronous calls after 20 warm-up steps:
     flowSteps(steps, 1e-3) for Line1d Quartic (a1 = a2 = 1) and QuarticGradient (k2 = k4 = 1) at
     N = 2^22 and Line2d QuarticGradient at 2048 x 2048; flowSteps(steps // 5) for Line1d LongRange
     (alpha = 1, k = 1, all pairs) at N = 16384; the no-passing minimiser (Line1d Nopassing, N = 2^17)
-    after a +0.5 frame jump, bounded at 5000 sweeps.  A failure is recorded, not raised."""
+    after a +0.5 frame jump, bounded at 5000 sweeps; Line1d Cuspy_Laplace_RandomForcing (mean 0,
+    stddev 0.05, forcing seed 0, every particle redrawn every 100 increments, first at a uniform
+    random increment in [0, 100)) at N = 2^22 (flowSteps(steps)) and at the reference example's
+    N = 1000 (flowSteps(5000); examples/Line1d_System_Cuspy_Laplace_RandomForcing.py)."""
     par = dict(eta=0.1, mu=1.0, dt=0.1, seed=2, distribution="weibull", parameters=[2.0, 1.0, 1e-5], offset=-100.0,
                nchunk=200)
     out = {}
@@ -276,6 +394,15 @@ def bench_next_rows(fqsb, n=2 ** 22, side=2048, n_lr=16384, n_np=2 ** 17, steps=
     flow("Line1d_Cuspy_LongRange", lambda: fqsb.Line1d.System_Cuspy_LongRange(
         m=1.0, k_interactions=1.0, alpha=1.0, k_frame=1.0 / n_lr, shape=[n_lr], **par), n_lr, steps // 5,
         extra=lambda size, k, dt: {"pair_terms_per_s": size * (size - 1) * k / dt})
+
+    def thermal(size):
+        return fqsb.Line1d.System_Cuspy_Laplace_RandomForcing(
+            m=1.0, k_interactions=1.0, k_frame=1.0 / size, mean=0.0, stddev=0.05, seed_forcing=0,
+            dinc_init=np.random.default_rng(3).integers(0, 100, size), dinc=np.full(size, 100), shape=[size], **par)
+
+    flow("Line1d_Cuspy_Laplace_RandomForcing", lambda: thermal(n), n, steps,
+         extra=lambda size, k, dt: {"draws_per_s": size / 100 * k / dt})
+    flow("Line1d_Cuspy_Laplace_RandomForcing_N1000", lambda: thermal(1000), 1000, 5000)
     try:
         s = fqsb.Line1d.System_Cuspy_Laplace_Nopassing(mu=1.0, k_interactions=1.0, k_frame=1.0 / n_np, shape=[n_np],
                                                        **{k: v for k, v in par.items() if k not in ("eta", "dt", "mu")})
@@ -290,6 +417,12 @@ def bench_next_rows(fqsb, n=2 ** 22, side=2048, n_lr=16384, n_np=2 ** 17, steps=
         out["Line1d_Cuspy_Laplace_Nopassing"] = {"error": f"{type(e).__name__}: {e}"}
     return out
 
+
+FORM_FUNCS = {"small_system": bench_small, "line2d": bench_line2d, "batched": bench_batched,
+              "adjoint": bench_adjoint, "next_rows": bench_next_rows}
+
+
+# ------------------------------------------------------------------------------------------ CPU arms
 
 def cpu_baseline_sample(n_sample=2 ** 16, steps=3000, repeats=1):
     """Time the CPU oracle (loop-per-statement restatement of the reference, libm, sequential sums)
@@ -308,41 +441,61 @@ def cpu_baseline_sample(n_sample=2 ** 16, steps=3000, repeats=1):
     return n_sample * steps * repeats / dt, dt
 
 
-def _ref_worker(args):
-    n_sample, steps, nsteps_total, warm = args
-    from oracle import oracle as O
-
-    s = O.line1d("Cuspy", shape=[n_sample], k_frame=1.0 / n_sample, **PAR, sum_mode=O.SUM_SEQUENTIAL,
-                 math_mode=O.MATH_LIBM)
-    s.u = np.random.default_rng(1).normal(0.0, 0.1, n_sample)
-    for _ in range(warm):
-        s.flowSteps(steps, V_FRAME)
-    times = []
-    for _ in range(nsteps_total):
-        t0 = time.perf_counter()
-        s.flowSteps(steps, V_FRAME)
-        times.append(time.perf_counter() - t0)
-    return times
+def _mem_available_bytes():
+    try:
+        for line in pathlib.Path("/proc/meminfo").read_text().splitlines():
+            if line.startswith("MemAvailable:"):
+                return int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    return None
 
 
 def run_reference(args, rank, world):
-    """CPU reference arm: the reference path restated on the host (the reference's own build needs
-    prrng / xtensor / GooseFEM, absent here), one independent sample system per host core."""
+    """CPU reference arm on the GPU arm's workload: the reference's time-integration path restated in C
+    (the reference's own build needs prrng / xtensor / GooseFEM, absent here) and built with OpenMP, so
+    its per-particle loops run over all host cores (flowSteps has no reductions: the results equal the
+    single-threaded build's).  Same N = 2^22 ring, parameters, seeds and initial state as the GPU arm;
+    each bench step is flowSteps(k) with k sized so that the warm-up and timed steps take about two
+    minutes (the GPU arm's step is flowSteps(1000)); the metric is the same particle-steps/s."""
     if rank != 0:
         return
-    import multiprocessing as mp
-
     from oracle import oracle as O
 
-    O.build()
+    N = args.n
+    nchunk = args.nchunk
+    need = N * nchunk * 8 + 16 * N * 8
+    avail = _mem_available_bytes()
+    note = ""
+    if avail is not None and need > 0.8 * avail:
+        nchunk = max(34, int((0.8 * avail - 16 * N * 8) / (8 * N)))
+        note = (f"; {nchunk} instead of {args.nchunk} yield positions per particle held in host memory "
+                f"(the yield sequence and the trajectory do not depend on it)")
+    O.build(threads=True)
     cores = os.cpu_count() or 1
-    n_sample, steps = 2 ** 14, 200
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(cores) as pool:
-        res = pool.map(_ref_worker, [(n_sample, steps, args.steps, args.warmup)] * cores)
-    per_step = [max(r[i] for r in res) for i in range(args.steps)]
-    total_time = sum(per_step)
-    value = cores * n_sample * steps * args.steps / total_time
+    t0 = time.perf_counter()
+    s = O.line1d("Cuspy", shape=[N], k_frame=1.0 / N, **dict(PAR, nchunk=nchunk), sum_mode=O.SUM_SEQUENTIAL,
+                 math_mode=O.MATH_LIBM, threads=True)
+    s.u = np.random.default_rng(1).normal(0.0, 0.1, N)
+    t_build = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    s.flowSteps(10, V_FRAME)
+    rate = N * 10 / (time.perf_counter() - t0)
+    budget = 120.0 / (args.steps + args.warmup)
+    inner = int(min(INNER, max(10, round(budget * rate / N))))
+    for _ in range(args.warmup):
+        s.flowSteps(inner, V_FRAME)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        s.flowSteps(inner, V_FRAME)
+        times.append(time.perf_counter() - t0)
+    total_time = sum(times)
+    value = N * inner * args.steps / total_time
+    sample = (f"the full N={N} ring of the GPU arm's workload (same parameters, seeds and u0), each bench step "
+              f"flowSteps({inner}) instead of flowSteps({INNER}); the reference's path restated in C (oracle/), "
+              f"built -O2 -ffp-contract=off -fopenmp, {cores} threads over the per-particle loops; construction "
+              f"{t_build:.1f} s (untimed){note}")
     line = {
         "impl": "reference",
         "metric": METRIC,
@@ -357,15 +510,15 @@ def run_reference(args, rank, world):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": workload(args.n), "l2": "inputs larger than L2 on the GPU arm"},
-        "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": "port",
-                         "sample": f"{cores} independent systems of N={n_sample} (one per core), "
-                                   f"each step flowSteps({steps}); the reference's path restated in C "
-                                   "(oracle/), built -O2 -ffp-contract=off"},
+        "config": {"workload": workload(N), "particles": N, "time_steps_per_step": inner,
+                   "l2": "inputs larger than L2 on the GPU arm"},
+        "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
+
+# ------------------------------------------------------------------------------------------ main
 
 def main():
     ap = argparse.ArgumentParser()
@@ -377,7 +530,10 @@ def main():
     ap.add_argument("--nchunk", type=int, default=2000, help="yield positions per particle (profiling cases only)")
     ap.add_argument("--no-minimise", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-forms", action="store_true", help="skip the batched / adjoint / small-system extras")
+    ap.add_argument("--no-forms", action="store_true", help="skip every entry of `forms`")
+    ap.add_argument("--forms", default=",".join(FORMS), help=f"comma-separated subset of {','.join(FORMS)}")
+    ap.add_argument("--full", action="store_true", help="run the forms' protocols at their configured sizes")
+    ap.add_argument("--only-forms", action="store_true", help="skip the main workload; run the selected forms")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -401,6 +557,14 @@ def main():
         torch.cuda.set_device(0)
 
     import frictionqpotspringblock_gb300 as fqsb
+    from frictionqpotspringblock_gb300 import _capi
+
+    forms_sel = [] if args.no_forms else [f for f in args.forms.split(",") if f]
+    if args.only_forms:
+        forms = {f: _guard(FORM_FUNCS[f], fqsb, full=args.full) for f in forms_sel}
+        if rank == 0:
+            print(json.dumps({"forms": forms, "full": args.full}), flush=True)
+        return
 
     N = args.n
     par = dict(PAR)
@@ -474,16 +638,21 @@ def main():
         inc0 = system.inc
         ret = system.minimise(tol=1e-5)
         barrier()
-        minimise = {"seconds": time.perf_counter() - t0, "steps": system.inc - inc0, "ret": ret}
+        ms = time.perf_counter() - t0
+        steps = system.inc - inc0
+        minimise = {"seconds": ms, "steps": steps, "ret": ret, "us_per_step": 1e6 * ms / max(1, steps),
+                    "over_flow_step": (ms / max(1, steps)) / kernel_s}
+    del system
 
-    forms = {}
-    if not args.no_forms:
-        forms["batched"] = bench_batched(fqsb)
-        forms["adjoint"] = bench_adjoint(fqsb)
-        forms["small_system"] = bench_small(fqsb)
-        forms["next_rows"] = bench_next_rows(fqsb)
+    # ---- arithmetic peaks of this GPU (the fp64 roofline's denominator), measured here
+    fp64_peak = _guard(_capi.measure_arith, "add", 0, local_rank)
+    fp64_peak_mul = _guard(_capi.measure_arith, "mul", 0, local_rank)
+
+    forms = {f: _guard(FORM_FUNCS[f], fqsb, full=args.full) for f in forms_sel}
 
     if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
         return
     cpu = None
     if not args.no_cpu_baseline:
@@ -491,6 +660,11 @@ def main():
         cpu = {"value": v, "unit": "particle-steps/s", "cores": 1, "kind": "port",
                "sample": f"oracle (reference restated in C, loop per statement, libm, sequential sums), "
                          f"N=65536 ring of the same parameters, flowSteps(3000), {secs:.1f} s on 1 core"}
+    figs = profile_figures()
+    traffic = figs["traffic_bytes_per_launch"] / figs["traffic_particles"] * N
+    fp64_gops = FP64_OPS_PER_PARTICLE_STEP * N / kernel_s / 1e9
+    fp64_pipe_gops = FP64_PIPE_OPS_PER_PARTICLE_STEP * N / kernel_s / 1e9
+    peak_gops = fp64_peak if isinstance(fp64_peak, float) else None
     line = {
         "metric": METRIC,
         "value": value,
@@ -511,23 +685,23 @@ def main():
                 "d2h_bytes_per_step": 8 * N},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved_gbs / hbm_peak, "traffic": TRAFFIC_BYTES_PER_PARTICLE_STEP * N,
-                     "traffic_unit": "bytes per launch (ncu capture at N=2^21 scaled by N)", "peak_kind": peak_kind,
-                     "algorithmic_bytes_per_particle_step": BYTES_PER_PARTICLE_STEP,
-                     "kernel": "k_step_line<Cuspy, Laplace1d, units, 2 per thread>",
-                     "kernel_us": kernel_s * 1e6},
+                     "frac": achieved_gbs / hbm_peak, "traffic": traffic,
+                     "traffic_unit": "bytes per launch (ncu capture of " + STEP_PROFILE.name + ", scaled by N)",
+                     "peak_kind": peak_kind, "algorithmic_bytes_per_particle_step": BYTES_PER_PARTICLE_STEP,
+                     "kernel": "k_step_line<Cuspy, Laplace1d, 2 per thread>", "kernel_us": kernel_s * 1e6},
         "fp64": {"ops_per_particle_step": FP64_OPS_PER_PARTICLE_STEP,
                  "ops_on_fp64_pipe": FP64_PIPE_OPS_PER_PARTICLE_STEP,
                  "ops_on_integer_pipes": FP64_OPS_PER_PARTICLE_STEP - FP64_PIPE_OPS_PER_PARTICLE_STEP,
-                 "achieved_gops": FP64_OPS_PER_PARTICLE_STEP * N / kernel_s / 1e9,
-                 "fp64_pipe_gops": FP64_PIPE_OPS_PER_PARTICLE_STEP * N / kernel_s / 1e9,
-                 "peak_gops": 505.0, "peak_source": "profiles/fp64_throughput_gb300.md",
-                 "frac": FP64_OPS_PER_PARTICLE_STEP * N / kernel_s / 1e9 / 505.0,
-                 "frac_fp64_pipe": FP64_PIPE_OPS_PER_PARTICLE_STEP * N / kernel_s / 1e9 / 505.0},
+                 "achieved_gops": fp64_gops, "fp64_pipe_gops": fp64_pipe_gops,
+                 "peak_gops": fp64_peak, "peak_mul_gops": fp64_peak_mul,
+                 "peak_source": "fqsb_measure_arith in this run (8 independent DADD chains per thread)",
+                 "frac": fp64_gops / peak_gops if peak_gops else None,
+                 "frac_fp64_pipe": fp64_pipe_gops / peak_gops if peak_gops else None},
         "clocks": clk,
         "wall_s": t_wall,
         "minimise": minimise,
         "forms": forms,
+        "forms_full": args.full,
         "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)

@@ -425,16 +425,27 @@ static double reduce(oq_system* s, const double* x, int square)
     while (P < N) {
         P *= 2;
     }
-    ensure_tmp(s, P);
+    ensure_tmp(s, P + P / 2 + 1);
+    double* t = s->tmp;
+    OQ_PARALLEL_FOR
     for (int64_t i = 0; i < P; ++i) {
-        s->tmp[i] = i < N ? (square ? x[i] * x[i] : x[i]) : 0.0;
+        t[i] = i < N ? (square ? x[i] * x[i] : x[i]) : 0.0;
     }
+    /* level by level into the other half of the scratch: within a level every pair is independent,
+     * so the threaded build splits the pairs over the threads and keeps the order of additions */
+    double* a = t;
+    double* b = t + P;
     for (int64_t len = P; len > 1; len /= 2) {
-        for (int64_t i = 0; i < len / 2; ++i) {
-            s->tmp[i] = s->tmp[2 * i] + s->tmp[2 * i + 1];
+        const int64_t h = len / 2;
+        OQ_PARALLEL_FOR
+        for (int64_t i = 0; i < h; ++i) {
+            b[i] = a[2 * i] + a[2 * i + 1];
         }
+        double* c = a;
+        a = b;
+        b = c;
     }
-    return s->tmp[0];
+    return a[0];
 }
 
 /* --------------------------------------------------------- forces */

@@ -277,11 +277,11 @@ class System:
     f_interactions = property(lambda s: s._get(F_INT))
     f_frame = property(lambda s: s._get(F_FRAME))
     f_damping = property(lambda s: s._get(F_DAMP))
-    temperature = property(lambda s: self._L.oq_get_scalar(s._h, S_TEMPERATURE))
-    residual = property(lambda s: self._L.oq_get_scalar(s._h, S_RESIDUAL))
-    mean_f_frame = property(lambda s: self._L.oq_get_scalar(s._h, S_MEAN_F_FRAME))
-    quasistaticActivityFirst = property(lambda s: self._L.oq_quasistatic_first(s._h))
-    quasistaticActivityLast = property(lambda s: self._L.oq_quasistatic_last(s._h))
+    temperature = property(lambda s: s._L.oq_get_scalar(s._h, S_TEMPERATURE))
+    residual = property(lambda s: s._L.oq_get_scalar(s._h, S_RESIDUAL))
+    mean_f_frame = property(lambda s: s._L.oq_get_scalar(s._h, S_MEAN_F_FRAME))
+    quasistaticActivityFirst = property(lambda s: s._L.oq_quasistatic_first(s._h))
+    quasistaticActivityLast = property(lambda s: s._L.oq_quasistatic_last(s._h))
 
     @property
     def u_frame(self):
