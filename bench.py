@@ -305,9 +305,10 @@ def bench_adjoint(fqsb, full=False, N=65536, T=5000, K=100, last=500):
     Weibull(2,1)+1e-5 seed 4, u0 = v0 = 0, u_frame(t) = 1e-3 t + 0.05 sin(2 pi t / 500), T = 5000,
     checkpoints every 100 steps; forward vs forward + backward wall time.  Gradient check: central
     finite differences (h = 1e-6) of the forward's loss along mu, k_interactions and eta, and along one
-    random direction (seed 9, unit max-norm) of u0, v0 and the schedule each; relative error against the
-    adjoint's directional derivative.  `fd_noise` is the finite difference's own resolution: the loss
-    rounded at 4 ulp, divided by h."""
+    random direction (seed 9, entries uniform in [0, 1)) of u0, v0 and the schedule each; relative error
+    against the adjoint's directional derivative.  `fd_noise_rel` is the finite difference's own
+    resolution relative to that derivative: 64 ulp of the loss (a sum of 500 x 65536 frame forces),
+    divided by h."""
     s = fqsb.Line1d.System_Smooth_Laplace(m=1.0, eta=0.1, mu=1.0, k_interactions=1.0, k_frame=1.0 / N, dt=0.1,
                                           shape=[N], seed=4, distribution="weibull", parameters=[2.0, 1.0, 1e-5],
                                           offset=-100.0, nchunk=1000)
@@ -334,7 +335,7 @@ def bench_adjoint(fqsb, full=False, N=65536, T=5000, K=100, last=500):
     out = {"particles": N, "steps": T, "checkpoint_every": K, "loss": L0, "forward_s": tf, "backward_s": tb,
            "backward_over_forward": tb / tf, "total_over_forward": (tf + tb) / tf}
     h = 1e-6
-    noise = 4 * np.spacing(abs(L0)) / h
+    noise = 64 * np.spacing(abs(L0)) / h
     checks = {}
     for i, name in enumerate(["mu", "k_interactions", "eta"]):
         e = np.zeros(3)
@@ -344,8 +345,7 @@ def bench_adjoint(fqsb, full=False, N=65536, T=5000, K=100, last=500):
                         "fd_noise_rel": noise / abs(gp[i])}
     rng = np.random.default_rng(9)
     for name, g, x in [("u0", gu, zero), ("v0", gv, zero), ("schedule", gs, sched)]:
-        d = rng.uniform(-1.0, 1.0, x.shape)
-        d /= np.max(np.abs(d))
+        d = rng.uniform(0.0, 1.0, x.shape)
         kw_p = {"u0": "u0", "v0": "v0", "schedule": "sc"}[name]
         fd = (loss(**{kw_p: x + h * d}) - loss(**{kw_p: x - h * d})) / (2 * h)
         an = float(np.dot(g.ravel(), d.ravel()))

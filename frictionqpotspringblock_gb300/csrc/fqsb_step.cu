@@ -340,13 +340,13 @@ __device__ __forceinline__ bool non_finite(double x)
 }
 
 /*
- * Per-particle well check; returns the (possibly refreshed) well cache.  `regen` is set when the
- * particle's chunk window must move; the pass-1 caller then marks its CTA pending.
+ * Per-particle well check of the cached well w (particle p's record, loaded by the caller); returns the
+ * (possibly refreshed) well cache.  `regen` is set when the particle's chunk window must move; the
+ * pass-1 caller then marks its CTA pending.
  */
 __device__ __forceinline__ double4_32a well_of(const DevSys& s, int64_t p, double un, bool act, StepShared& sh,
-                                               bool& regen)
+                                               bool& regen, double4_32a w)
 {
-    double4_32a w = s.wc[p];
     regen = false;
     if (!in_well(w.x, w.y, un) && !non_finite(un)) {
         int64_t gold = s.gidx[p];
@@ -365,6 +365,12 @@ __device__ __forceinline__ double4_32a well_of(const DevSys& s, int64_t p, doubl
         }
     }
     return w;
+}
+
+__device__ __forceinline__ double4_32a well_of(const DevSys& s, int64_t p, double un, bool act, StepShared& sh,
+                                               bool& regen)
+{
+    return well_of(s, p, un, act, sh, regen, s.wc[p]);
 }
 
 /* Role of the CTA epilogue in the step's kernels. */
@@ -491,6 +497,15 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_line(DevSys s
     double* a1 = s.a[cur ^ 1];
 
     double un[PPT], vr[PPT], ar[PPT];
+    /* the cached wells are loaded together with the state, so that their latency overlaps the
+     * position update and the neighbour exchange instead of following them */
+    double4_32a wpre[PPT];
+#pragma unroll
+    for (int j = 0; j < PPT; ++j) {
+        if (p0 + j < N) {
+            wpre[j] = s.wc[p0 + j];
+        }
+    }
     if (PPT == 2) {
         double2 uu = *reinterpret_cast<const double2*>(u0 + p0);
         double2 vv = *reinterpret_cast<const double2*>(v0 + p0);
@@ -530,7 +545,7 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_line(DevSys s
         }
         double up = un[j];
         bool regen;
-        double4_32a w = well_of(s, p, up, act, sh, regen);
+        double4_32a w = well_of(s, p, up, act, sh, regen, wpre[j]);
         pending |= regen;
         double ff;
         double sfp = frame_pot<POT, SOFT>(s, w, up, uf, ff);

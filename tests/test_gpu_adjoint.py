@@ -184,3 +184,111 @@ def test_autograd_cuda_tensors():
         out.append([loss.detach().cpu()] + [x.grad.detach().cpu() for x in (tu0, tv0, tsch, tpar)])
     for a, b in zip(*out):
         assert torch.equal(a, b)
+
+
+def torch_loss_schedule(kind, yl, yr, u0, v0, sched, params, kf, last, kappa=1.0, segment=100):
+    """torch_loss for any size: the unrolled FP64 forward on u0's device with the forward's wells, in
+    checkpointed segments of `segment` steps (autograd recomputes each segment in the backward)."""
+    from torch.utils.checkpoint import checkpoint
+
+    mu, k, eta = params[0], params[1], params[2]
+    m, dt = 1.0, 0.1
+    T = sched.shape[0]
+
+    def seg(u, v, a, acc, t0, t1):
+        for t in range(t0, t1):
+            up = (u + dt * v) + ((0.5 * dt) * dt) * a
+            if kind == "Smooth":
+                umin = 0.5 * (yl + yr)
+                dy = 0.5 * (yr - yl)
+                fp = -mu * dy / math.pi * torch.sin(math.pi * (up - umin) / dy)
+            else:
+                xi = 0.5 * (yl + yr)
+                u_r = (mu * xi + kappa * yr) / (mu + kappa)
+                u_l = (mu * xi + kappa * yl) / (mu + kappa)
+                fp = torch.where(up < u_l, kappa * (up - yl),
+                                 torch.where(up <= u_r, mu * (0.5 * (yl + yr) - up), kappa * (up - yr)))
+            fi = k * ((torch.roll(up, 1) - 2 * up) + torch.roll(up, -1))
+            ff = kf * (sched[t] - up)
+            s = (ff + fp) + fi
+            v1 = v + dt * a
+            a1 = (s + (-eta) * v1) / m
+            v2 = v + (0.5 * dt) * (a + a1)
+            a2 = (s + (-eta) * v2) / m
+            v3 = v + (0.5 * dt) * (a + a2)
+            a3 = (s + (-eta) * v3) / m
+            if t >= T - last:
+                acc = acc + torch.mean(ff)
+            u, v, a = up, v3, a3
+        return u, v, a, acc
+
+    u, v, a = u0, v0, torch.zeros_like(u0)
+    acc = torch.zeros((), dtype=torch.float64, device=u0.device)
+    for t0 in range(0, T, segment):
+        u, v, a, acc = checkpoint(seg, u, v, a, acc, t0, min(T, t0 + segment), use_reentrant=False)
+    return acc / last + 0.5 * torch.mean(u * u)
+
+
+@pytest.mark.timeout(1800)
+@pytest.mark.parametrize("kind", ["Smooth", "SemiSmooth"])
+def test_adjoint_full_size(kind):
+    """The differentiation workload at its own size: Line1d System_{Smooth,SemiSmooth}_Laplace (kappa = 1),
+    N = 65536, m = 1, eta = 0.1, mu = 1, k = 1, k_frame = 1/N, dt = 0.1, Weibull(2,1)+1e-5 from pcg32
+    seed 4, u0 = v0 = 0, T = 5000 steps with u_frame(t) = 1e-3 t + 0.05 sin(2 pi t / 500), loss = mean
+    f_frame over the last 500 steps + 0.5 mean(u_T^2), checkpoints every 100 steps.
+    (1) Against torch autograd through the unrolled FP64 step on the GPU (wells held, and checked to
+    stay): relative error of every gradient below 1e-9.  (2) Against central finite differences of
+    the library's forward, h = 1e-6: along mu and k_interactions within 1e-6 relative; along eta and
+    along one random direction (entries uniform in [0, 1)) of u0, v0 and the schedule within 1e-6
+    relative plus the finite difference's own resolution, 64 ulp(loss) / h: the loss sums 500 x 65536
+    frame forces, so its rounding reaches a few dozen ulp, and these derivatives (1e-10 to 1e-7) are
+    below what a difference quotient with h = 1e-6 resolves to 1e-6."""
+    N, T, Kc, last = 65536, 5000, 100, 500
+    par = dict(m=1.0, eta=0.1, mu=1.0, k_interactions=1.0, k_frame=1.0 / N, dt=0.1, shape=[N], seed=4,
+               distribution="weibull", parameters=[2.0, 1.0, 1e-5], offset=-100.0, nchunk=1000)
+    system = (fqsb.Line1d.System_Smooth_Laplace(**par) if kind == "Smooth"
+              else fqsb.Line1d.System_SemiSmooth_Laplace(kappa=1.0, **par))
+    t = np.arange(T)
+    sched = 1e-3 * t + 0.05 * np.sin(2 * np.pi * t / 500)
+    params = np.array([1.0, 1.0, 0.1])
+    zero = np.zeros(N)
+
+    def L(u0=zero, v0=zero, sc=sched, p=params):
+        system.set_parameters(*p)
+        system.u, system.v, system.a = u0, v0, zero
+        return system.adjoint_forward(sc, K=Kc, last=last)
+
+    i0 = system.chunk.index_at_align.copy()
+    yl = torch.tensor(system.chunk.left_of_align, dtype=torch.float64, device="cuda")
+    yr = torch.tensor(system.chunk.right_of_align, dtype=torch.float64, device="cuda")
+    L0 = L()
+    assert np.array_equal(system.chunk.index_at_align, i0), "a particle changed well: the torch check holds wells"
+    gu, gv, gs, gp = system.adjoint_backward()
+
+    tu0 = torch.zeros(N, dtype=torch.float64, device="cuda", requires_grad=True)
+    tv0 = torch.zeros(N, dtype=torch.float64, device="cuda", requires_grad=True)
+    tsch = torch.tensor(sched, device="cuda", requires_grad=True)
+    tpar = torch.tensor(params, device="cuda", requires_grad=True)
+    ref = torch_loss_schedule(kind, yl, yr, tu0, tv0, tsch, tpar, 1.0 / N, last)
+    ref.backward()
+    assert abs(L0 - ref.item()) <= 1e-12 * abs(ref.item())
+    for a, b, name in zip([gu, gv, gs, gp], [tu0.grad, tv0.grad, tsch.grad, tpar.grad],
+                          ["u0", "v0", "schedule", "params"]):
+        b = b.cpu().numpy()
+        err = np.linalg.norm(a.ravel() - b.ravel()) / np.linalg.norm(b)
+        assert err < 1e-9, (name, err)
+
+    h = 1e-6
+    noise = 64 * np.spacing(abs(L0)) / h
+    for i, name in enumerate(["mu", "k_interactions", "eta"]):
+        e = np.zeros(3)
+        e[i] = h
+        fd = (L(p=params + e) - L(p=params - e)) / (2 * h)
+        tol = 1e-6 * abs(gp[i]) + (noise if name == "eta" else 0.0)
+        assert abs(fd - gp[i]) <= tol, (name, fd, gp[i], noise)
+    rng = np.random.default_rng(9)
+    for name, g, x in [("u0", gu, zero), ("v0", gv, zero), ("sc", gs, sched)]:
+        d = rng.uniform(0.0, 1.0, x.shape)
+        fd = (L(**{name: x + h * d}) - L(**{name: x - h * d})) / (2 * h)
+        an = float(np.dot(g.ravel(), d.ravel()))
+        assert abs(fd - an) <= 1e-6 * abs(an) + noise, (name, fd, an, noise)
