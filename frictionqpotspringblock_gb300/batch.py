@@ -148,3 +148,25 @@ class Line1d_System_Cuspy_Laplace:
         out = np.empty(len(self._sizes))
         self._check(C.lib().fqsb_batch_frame(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
         return out
+
+
+def quasistatic_shard(sizes, seeds, k_frame, rank: int, world: int, ncycles: int, eps: float, tol: float = 1e-5,
+                      niter_tol: int = 10, max_iter: int = int(1e9), device: int = 0, **kwargs):
+    """One rank's part of a sharded batch: the realisations partition(sizes, world)[rank] as one batch on
+    `device`, run through `ncycles` quasistatic cycles.  Returns (idx, result) with result as
+    Line1d_System_Cuspy_Laplace.quasistatic gives it for those realisations (rows in idx order).  The
+    ranks exchange nothing while they run: gathering the per-realisation results (by idx) is the
+    caller's, e.g. with torch.distributed.all_gather_object.  kwargs: the shared constructor
+    parameters of Line1d_System_Cuspy_Laplace."""
+    sizes = np.asarray(sizes, dtype=np.int64)
+    seeds = np.asarray(np.broadcast_to(seeds, sizes.shape), dtype=np.uint64)
+    k_frame = np.asarray(np.broadcast_to(k_frame, sizes.shape), dtype=np.float64)
+    idx = partition(sizes, world)[rank]
+    if len(idx) == 0:
+        empty = np.empty((0, ncycles))
+        return idx, {"u_frame": empty, "f_frame": empty, "S": empty.astype(np.int64), "inc": empty.astype(np.int64),
+                     "status": np.empty(0, np.int32)}
+    b = Line1d_System_Cuspy_Laplace(sizes[idx], seeds[idx], k_frame[idx], device=device, **kwargs)
+    out = b.quasistatic(ncycles, eps, tol=tol, niter_tol=niter_tol, max_iter=max_iter)
+    del b
+    return idx, out

@@ -399,6 +399,11 @@ __device__ __forceinline__ void step_epilogue(const DevSys& s, StepShared& sh, i
     int tid = threadIdx.x + threadIdx.y * blockDim.x;
     int64_t bid = blockIdx.x + (int64_t)blockIdx.y * gridDim.x;
     Ctl* c = s.ctl;
+    /* without a residual tree the rest is thread 0's work: the other threads leave now instead of
+     * waiting for its atomics (their registers go back to the SM for the next CTAs) */
+    if (!tree && tid != 0) {
+        return;
+    }
     if (tid == 0) {
         if (tree) {
             s.partials[bid] = make_double2(sf, sff);
@@ -426,7 +431,9 @@ __device__ __forceinline__ void step_epilogue(const DevSys& s, StepShared& sh, i
             sh.last = (t == gridDim.x * gridDim.y - 1) ? 1 : 0;
         }
     }
-    __syncthreads();
+    if (tree) {
+        __syncthreads();
+    }
     if (!sh.last) {
         return;
     }
@@ -445,7 +452,7 @@ __device__ __forceinline__ void step_epilogue(const DevSys& s, StepShared& sh, i
         }
     }
     double2 tot = make_double2(0.0, 0.0);
-    if (resid) {
+    if (tree) {
         tot = tree_partials(s.partials, (int64_t)gridDim.x * gridDim.y, sh.red);
     }
     if (tid == 0) {
@@ -466,6 +473,21 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_line(DevSys s
 {
     __shared__ StepShared sh;
     __shared__ double sh_un[256 * PPT];
+    const int64_t N = s.N;
+    const int T = blockDim.x;
+    const int64_t base = (int64_t)blockIdx.x * T * PPT;
+    const int64_t p0 = base + (int64_t)threadIdx.x * PPT;
+    /* the cached wells do not depend on the run state: their loads are issued first, so that their
+     * latency overlaps the run-state read, the state loads and the position update */
+    double4_32a wpre[PPT];
+    if (!redo) {
+#pragma unroll
+        for (int j = 0; j < PPT; ++j) {
+            if (p0 + j < N) {
+                wpre[j] = s.wc[p0 + j];
+            }
+        }
+    }
     if (!step_prologue(s, sh, true)) {
         return;
     }
@@ -477,6 +499,13 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_line(DevSys s
         if (threadIdx.x == 0) {
             s.cta_pending[blockIdx.x] = 0;
         }
+        /* after the regeneration kernel moved windows */
+#pragma unroll
+        for (int j = 0; j < PPT; ++j) {
+            if (p0 + j < N) {
+                wpre[j] = s.wc[p0 + j];
+            }
+        }
     }
     const int cur = sh.cur;
     const bool act = (sh.flags & (RF_ACT | RF_TRUNCATE | RF_EVENT)) != 0;
@@ -485,10 +514,6 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_line(DevSys s
     const bool record = (sh.flags & RF_RECORD) != 0;
     const int64_t rec_step = record ? ((volatile Ctl*)s.ctl)->step : 0;
     const double uf = sh.uf;
-    const int64_t N = s.N;
-    const int T = blockDim.x;
-    const int64_t base = (int64_t)blockIdx.x * T * PPT;
-    const int64_t p0 = base + (int64_t)threadIdx.x * PPT;
     const double* u0 = s.u[cur];
     const double* v0 = s.v[cur];
     const double* a0 = s.a[cur];
@@ -497,15 +522,6 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_line(DevSys s
     double* a1 = s.a[cur ^ 1];
 
     double un[PPT], vr[PPT], ar[PPT];
-    /* the cached wells are loaded together with the state, so that their latency overlaps the
-     * position update and the neighbour exchange instead of following them */
-    double4_32a wpre[PPT];
-#pragma unroll
-    for (int j = 0; j < PPT; ++j) {
-        if (p0 + j < N) {
-            wpre[j] = s.wc[p0 + j];
-        }
-    }
     if (PPT == 2) {
         double2 uu = *reinterpret_cast<const double2*>(u0 + p0);
         double2 vv = *reinterpret_cast<const double2*>(v0 + p0);

@@ -186,9 +186,11 @@ def test_autograd_cuda_tensors():
         assert torch.equal(a, b)
 
 
-def torch_loss_schedule(kind, yl, yr, u0, v0, sched, params, kf, last, kappa=1.0, segment=100):
-    """torch_loss for any size: the unrolled FP64 forward on u0's device with the forward's wells, in
-    checkpointed segments of `segment` steps (autograd recomputes each segment in the backward)."""
+def torch_loss_schedule(kind, data, u0, v0, sched, params, kf, last, kappa=1.0, segment=100):
+    """The unrolled FP64 forward in torch on u0's device for any size, in checkpointed segments of
+    `segment` steps (autograd recomputes each segment in the backward).  The well of every particle is
+    looked up at every step from its chunk row data [N, W] (y[i] <= u < y[i+1], the align rule), so
+    particles may change well as in the library's forward; the index has zero derivative."""
     from torch.utils.checkpoint import checkpoint
 
     mu, k, eta = params[0], params[1], params[2]
@@ -198,6 +200,9 @@ def torch_loss_schedule(kind, yl, yr, u0, v0, sched, params, kf, last, kappa=1.0
     def seg(u, v, a, acc, t0, t1):
         for t in range(t0, t1):
             up = (u + dt * v) + ((0.5 * dt) * dt) * a
+            i = torch.searchsorted(data, up.detach().unsqueeze(1), right=True) - 1
+            yl = torch.gather(data, 1, i).squeeze(1)
+            yr = torch.gather(data, 1, i + 1).squeeze(1)
             if kind == "Smooth":
                 umin = 0.5 * (yl + yr)
                 dy = 0.5 * (yr - yl)
@@ -234,42 +239,47 @@ def torch_loss_schedule(kind, yl, yr, u0, v0, sched, params, kf, last, kappa=1.0
 def test_adjoint_full_size(kind):
     """The differentiation workload at its own size: Line1d System_{Smooth,SemiSmooth}_Laplace (kappa = 1),
     N = 65536, m = 1, eta = 0.1, mu = 1, k = 1, k_frame = 1/N, dt = 0.1, Weibull(2,1)+1e-5 from pcg32
-    seed 4, u0 = v0 = 0, T = 5000 steps with u_frame(t) = 1e-3 t + 0.05 sin(2 pi t / 500), loss = mean
-    f_frame over the last 500 steps + 0.5 mean(u_T^2), checkpoints every 100 steps.
-    (1) Against torch autograd through the unrolled FP64 step on the GPU (wells held, and checked to
-    stay): relative error of every gradient below 1e-9.  (2) Against central finite differences of
-    the library's forward, h = 1e-6: along mu and k_interactions within 1e-6 relative; along eta and
-    along one random direction (entries uniform in [0, 1)) of u0, v0 and the schedule within 1e-6
-    relative plus the finite difference's own resolution, 64 ulp(loss) / h: the loss sums 500 x 65536
-    frame forces, so its rounding reaches a few dozen ulp, and these derivatives (1e-10 to 1e-7) are
-    below what a difference quotient with h = 1e-6 resolves to 1e-6."""
+    seed 4, T = 5000 steps with u_frame(t) = 1e-3 t + 0.05 sin(2 pi t / 500), loss = mean f_frame over
+    the last 500 steps + 0.5 mean(u_T^2), checkpoints every 100 steps; u0 = the equilibrium at
+    u_frame = 0 (minimise from u = v = 0), v0 = 0.  (From u = 0 itself many particles start near a
+    potential maximum and fall to either side: the loss then changes by finite amounts under 1e-6
+    perturbations, and no finite difference resolves a derivative.)  A few particles still change well
+    during the run (quasistatic slips).
+    (1) Against torch autograd through the unrolled FP64 step on the GPU, with every particle's well
+    looked up at every step as the forward does: relative error of every gradient below 1e-9.
+    (2) Against central finite differences of the library's forward, h = 1e-6: along mu,
+    k_interactions and eta, and along one random direction (entries uniform in [0, 1)) of u0, v0 and
+    the schedule, within 1e-6 relative plus the finite difference's own resolution, 64 ulp(loss) / h
+    (the loss sums 500 x 65536 frame forces, so its rounding reaches a few dozen ulp)."""
     N, T, Kc, last = 65536, 5000, 100, 500
     par = dict(m=1.0, eta=0.1, mu=1.0, k_interactions=1.0, k_frame=1.0 / N, dt=0.1, shape=[N], seed=4,
                distribution="weibull", parameters=[2.0, 1.0, 1e-5], offset=-100.0, nchunk=1000)
     system = (fqsb.Line1d.System_Smooth_Laplace(**par) if kind == "Smooth"
               else fqsb.Line1d.System_SemiSmooth_Laplace(kappa=1.0, **par))
+    system.minimise(max_iter=1000000)
+    ueq = system.u
     t = np.arange(T)
     sched = 1e-3 * t + 0.05 * np.sin(2 * np.pi * t / 500)
     params = np.array([1.0, 1.0, 0.1])
     zero = np.zeros(N)
 
-    def L(u0=zero, v0=zero, sc=sched, p=params):
+    def L(u0=ueq, v0=zero, sc=sched, p=params):
         system.set_parameters(*p)
         system.u, system.v, system.a = u0, v0, zero
         return system.adjoint_forward(sc, K=Kc, last=last)
 
-    i0 = system.chunk.index_at_align.copy()
-    yl = torch.tensor(system.chunk.left_of_align, dtype=torch.float64, device="cuda")
-    yr = torch.tensor(system.chunk.right_of_align, dtype=torch.float64, device="cuda")
+    system.u = ueq
+    start = system.chunk.start.copy()
+    data = torch.tensor(system.chunk.data, dtype=torch.float64, device="cuda")
     L0 = L()
-    assert np.array_equal(system.chunk.index_at_align, i0), "a particle changed well: the torch check holds wells"
+    assert np.array_equal(system.chunk.start, start), "a chunk window moved: the torch restatement reads one window"
     gu, gv, gs, gp = system.adjoint_backward()
 
-    tu0 = torch.zeros(N, dtype=torch.float64, device="cuda", requires_grad=True)
+    tu0 = torch.tensor(ueq, device="cuda", requires_grad=True)
     tv0 = torch.zeros(N, dtype=torch.float64, device="cuda", requires_grad=True)
     tsch = torch.tensor(sched, device="cuda", requires_grad=True)
     tpar = torch.tensor(params, device="cuda", requires_grad=True)
-    ref = torch_loss_schedule(kind, yl, yr, tu0, tv0, tsch, tpar, 1.0 / N, last)
+    ref = torch_loss_schedule(kind, data, tu0, tv0, tsch, tpar, 1.0 / N, last)
     ref.backward()
     assert abs(L0 - ref.item()) <= 1e-12 * abs(ref.item())
     for a, b, name in zip([gu, gv, gs, gp], [tu0.grad, tv0.grad, tsch.grad, tpar.grad],
@@ -284,10 +294,9 @@ def test_adjoint_full_size(kind):
         e = np.zeros(3)
         e[i] = h
         fd = (L(p=params + e) - L(p=params - e)) / (2 * h)
-        tol = 1e-6 * abs(gp[i]) + (noise if name == "eta" else 0.0)
-        assert abs(fd - gp[i]) <= tol, (name, fd, gp[i], noise)
+        assert abs(fd - gp[i]) <= 1e-6 * abs(gp[i]) + noise, (name, fd, gp[i], noise)
     rng = np.random.default_rng(9)
-    for name, g, x in [("u0", gu, zero), ("v0", gv, zero), ("sc", gs, sched)]:
+    for name, g, x in [("u0", gu, ueq), ("v0", gv, zero), ("sc", gs, sched)]:
         d = rng.uniform(0.0, 1.0, x.shape)
         fd = (L(**{name: x + h * d}) - L(**{name: x - h * d})) / (2 * h)
         an = float(np.dot(g.ravel(), d.ravel()))
