@@ -278,7 +278,13 @@ def bench_batched(fqsb, full=False):
     r = b.quasistatic(ncycles, 1e-5)
     t = time.perf_counter() - t0
     ps = int((r["inc"][:, -1] * sizes).sum())
-    out.update(seconds=t, particle_steps=ps, value=ps / t, converged=int(np.sum(r["status"] == 0)))
+    steps = r["inc"][:, -1]
+    out.update(seconds=t, particle_steps=ps, value=ps / t, converged=int(np.sum(r["status"] == 0)),
+               steps_per_realisation={"mean": float(steps.mean()), "max": int(steps.max()),
+                                      "min": int(steps.min())},
+               # particle-steps done / (the longest realisation's steps x all particles): the share of the
+               # launched tiles that had work, if every iteration launched every tile
+               busy_fraction=ps / (float(steps.max()) * float(sizes.sum())))
     del b
     pick = np.sort(np.random.default_rng(5).choice(4096, nloop, replace=False))
     tp, pps = 0.0, 0
