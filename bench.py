@@ -158,13 +158,15 @@ def _sync_seconds(t0):
 
 # ------------------------------------------------------------------------------------------ forms
 
-def bench_small(fqsb, full=False, cycles=100, cpu_cycles=10):
+def bench_small(fqsb, full=False, cycles=100, cpu_cycles=100):
     """Small system: Line1d System_Cuspy_Laplace N = 1024, m = 1, eta = 0.1, mu = 1, k = 1,
     k_frame = 1/1024, dt = 0.1, Weibull(2,1)+1e-5 seed 0, 1000-position chunk shifted per particle so
     that u = 0 is the centre of well 500; from u = v = 0, 100 cycles of eventDrivenStep(1e-5,
     kick=False), eventDrivenStep(1e-5, kick=True), minimise(tol=1e-5, max_iter=1e6).  The CPU oracle
-    (the reference restated: libm, sequential sums, one core) runs the first `cpu_cycles` cycles of the
-    same protocol; the GPU is timed over the same first cycles and over all 100."""
+    (the reference restated: libm, sequential sums, one core) runs the same protocol.  `sizes`: time
+    per time step of timeSteps(20000) and of a minimise after a +0.5 frame jump for N = 64 ... 16384
+    (offset -500, nchunk 1000, seed 0), on the one-cluster path and on the CUDA-graph path
+    (FQSB_NO_SMALL=1 at construction)."""
     N = 1024
     par = dict(m=1.0, eta=0.1, mu=1.0, k_interactions=1.0, k_frame=1.0 / N, dt=0.1, shape=[N], seed=0,
                distribution="weibull", parameters=[2.0, 1.0, 1e-5], nchunk=1000)
@@ -185,12 +187,12 @@ def bench_small(fqsb, full=False, cycles=100, cpu_cycles=10):
 
     s = fqsb.Line1d.System_Cuspy_Laplace(offset=0.0, offset_per_particle=offp, **par)
     assert np.all(s.chunk.index_at_align == 500)
-    t_first, steps_first = run(s, cpu_cycles)
-    t_rest, steps_rest = run(s, cycles - cpu_cycles)
+    t_first, steps_first = run(s, 10)
+    t_rest, steps_rest = run(s, cycles - 10)
     t, steps = t_first + t_rest, steps_first + steps_rest
     out = {"particles": N, "cycles": cycles, "seconds": t, "seconds_per_cycle": t / cycles, "time_steps": steps,
-           "us_per_step": 1e6 * t / steps, "first_cycles": {"cycles": cpu_cycles, "seconds": t_first,
-                                                             "time_steps": steps_first}}
+           "us_per_step": 1e6 * t / steps, "first_10_cycles": {"seconds": t_first, "time_steps": steps_first,
+                                                                "us_per_step": 1e6 * t_first / steps_first}}
     if cpu_cycles > 0:
         from oracle import oracle as O  # the CPU baseline: the reference restated, one core
 
@@ -199,7 +201,33 @@ def bench_small(fqsb, full=False, cycles=100, cpu_cycles=10):
         tc, sc = run(r, cpu_cycles)
         out["cpu_oracle"] = {"cycles": cpu_cycles, "cores": 1, "seconds": tc, "time_steps": sc,
                              "us_per_step": 1e6 * tc / sc}
-        out["speedup_vs_cpu_oracle_same_cycles"] = tc / t_first
+        if cpu_cycles == cycles:
+            out["speedup_vs_cpu_oracle"] = tc / t
+    sizes = {}
+    for path in ("cluster", "graph"):
+        for n in (64, 1024, 4096, 16384):
+            if path == "graph":
+                os.environ["FQSB_NO_SMALL"] = "1"
+            try:
+                q = fqsb.Line1d.System_Cuspy_Laplace(m=1.0, eta=0.1, mu=1.0, k_interactions=1.0, k_frame=1.0 / n,
+                                                     dt=0.1, shape=[n], seed=0, distribution="weibull",
+                                                     parameters=[2.0, 1.0, 1e-5], offset=-500.0, nchunk=1000)
+            finally:
+                os.environ.pop("FQSB_NO_SMALL", None)
+            q.flowSteps(100, 1e-3)
+            t0 = time.perf_counter()
+            q.timeSteps(20000)
+            t1 = time.perf_counter()
+            q.u_frame = q.u_frame + 0.5
+            i0 = q.inc
+            t2 = time.perf_counter()
+            q.minimise(max_iter=200000, max_iter_is_error=False)
+            t3 = time.perf_counter()
+            sizes[f"{path}_N{n}"] = {"time_steps_us_per_step": 1e6 * (t1 - t0) / 20000,
+                                     "minimise_us_per_step": 1e6 * (t3 - t2) / max(1, q.inc - i0),
+                                     "minimise_steps": q.inc - i0}
+            del q
+    out["sizes"] = sizes
     return out
 
 

@@ -590,16 +590,54 @@ __global__ void __launch_bounds__(128) k_batch_regen(BatchDev b)
 {
     const int nreg = b.run->n_regen;
     const DevSys& s = b.d;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nreg; k += gridDim.x * blockDim.x) {
-        int64_t g = b.regen_list[k];
-        int j = b.tile_inst[g / b.tile];
-        Inst* I = b.inst + j;
-        double x = s.u[I->cur ^ 1][g];
-        int64_t gold = s.gidx[g];
-        if (!dev_align(s, g, x)) {
-            atomicOr(&b.run->walk_flag, 1);
+    if (nreg >= (int)(gridDim.x * blockDim.x) / 4) {
+        /* many moves: one thread per particle */
+        for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nreg; k += gridDim.x * blockDim.x) {
+            int64_t g = b.regen_list[k];
+            int j = b.tile_inst[g / b.tile];
+            Inst* I = b.inst + j;
+            double x = s.u[I->cur ^ 1][g];
+            int64_t gold = s.gidx[g];
+            if (!dev_align(s, g, x)) {
+                atomicOr(&b.run->walk_flag, 1);
+            }
+            atomicAdd((unsigned long long*)&I->s_signed, (unsigned long long)(s.gidx[g] - gold));
         }
-        atomicAdd((unsigned long long*)&I->s_signed, (unsigned long long)(s.gidx[g] - gold));
+        return;
+    }
+    /* few moves: one CTA per particle, its threads sharing the draws (fwd_move_*); the same values */
+    __shared__ FwdMove m_sh;
+    __shared__ int ok_sh;
+    __shared__ long long gold_sh;
+    const uint64_t mv_c = pcg_advance(0ULL, (uint64_t)blockDim.x);
+    const uint64_t mv_a = pcg_advance(1ULL, (uint64_t)blockDim.x) - mv_c;
+    for (int k = blockIdx.x; k < nreg; k += gridDim.x) {
+        const int64_t g = b.regen_list[k];
+        Inst* I = b.inst + b.tile_inst[g / b.tile];
+        if (threadIdx.x == 0) {
+            double x = s.u[I->cur ^ 1][g];
+            gold_sh = s.gidx[g];
+            FwdMove m;
+            ok_sh = fwd_move_plan(s, g, x, m) ? 1 : 0;
+            if (ok_sh) {
+                m_sh = m;
+            }
+            else if (!dev_align(s, g, x)) {
+                atomicOr(&b.run->walk_flag, 1);
+            }
+        }
+        __syncthreads();
+        if (ok_sh) {
+            fwd_move_draws(s, m_sh, (int)threadIdx.x, (int)blockDim.x, mv_a, mv_c);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            if (ok_sh) {
+                fwd_move_sum(s, m_sh);
+            }
+            atomicAdd((unsigned long long*)&I->s_signed, (unsigned long long)(s.gidx[g] - gold_sh));
+        }
+        __syncthreads();
     }
 }
 

@@ -614,6 +614,127 @@ static __device__ __noinline__ bool dev_align(const DevSys& s, int64_t p, double
     return true;
 }
 
+/*
+ * Cooperative forward window move.  A move costs W - keep draws, each a distribution transform of
+ * some hundred dependent fp64 operations (the portable double-double log of the Weibull / exponential
+ * transforms); one thread doing them alone stalls its CTA (and, in the one-cluster kernel, the whole
+ * cluster) for ~1 ms.  The draws are independent given their pcg32 states, so the threads of a CTA
+ * share them; only the running sum, one addition per value, stays with the particle's own thread and
+ * runs in the sequence's order -- the values are the ones dev_align writes, bit for bit.
+ *
+ * Applies when u lies inside the window but its index has passed the upper margin (the usual way a
+ * particle leaves its window in a dynamic run) and the forward walker is exact from the window end;
+ * every other move goes through dev_align.
+ */
+struct FwdMove {
+    int64_t p, ns, keep;
+    uint64_t st_first; /* pcg32 state whose output is the draw of index old end + 1 */
+};
+
+/* Plans the move of particle p to target u; on success also copies the kept values down. */
+__device__ __forceinline__ bool fwd_move_plan(const DevSys& s, int64_t p, double u, FwdMove& m)
+{
+    if (!(u == u)) {
+        return false;
+    }
+    const int64_t W = s.W;
+    double* y = s.data + p * W;
+    if (!(y[0] <= u && u < y[W - 1])) {
+        return false;
+    }
+    int64_t li = s.cidx[p];
+    if (y[li] <= u) {
+        while (li + 1 < W && y[li + 1] <= u) {
+            ++li;
+        }
+    }
+    else {
+        while (li > 0 && y[li] > u) {
+            --li;
+        }
+    }
+    if (li < W - s.buffer) {
+        return false; /* inside the margins, or a move down */
+    }
+    const int64_t start = s.start[p];
+    const int64_t ns = start + li - s.margin;
+    const int64_t end = start + W - 1;
+    const int64_t keep = end + 1 - ns;
+    int kind;
+    int64_t ko;
+    uint64_t sto;
+    seq_origin(s, p, kind, ko, sto);
+    if (ns <= start || keep <= 0 || end < ko) {
+        return false;
+    }
+    for (int64_t j = 0; j < keep; ++j) {
+        y[j] = y[j + (ns - start)];
+    }
+    m.p = p;
+    m.ns = ns;
+    m.keep = keep;
+    m.st_first = pcg_advance(sto, (uint64_t)(end + 1 - ko));
+    return true;
+}
+
+/* Draws of one planned move: thread `lane` of `nlanes` writes the draws of window slots
+ * keep + lane, keep + lane + nlanes, ... (one jump-ahead, then strides of nlanes steps: the
+ * stride map x -> a x + c with c = advance(0, nlanes), a = advance(1, nlanes) - c). */
+__device__ __forceinline__ void fwd_move_draws(const DevSys& s, const FwdMove& m, int lane, int nlanes, uint64_t sa,
+                                               uint64_t sc)
+{
+    const int64_t W = s.W;
+    double* y = s.data + m.p * W;
+    uint64_t st = pcg_advance(m.st_first, (uint64_t)lane);
+    for (int64_t j = m.keep + lane; j < W; j += nlanes) {
+        y[j] = dev_draw(s, st);
+        st = sa * st + sc;
+    }
+}
+
+/* The running sum of one planned move over its drawn slots, in the sequence's order (walker_next's
+ * rules), then the particle's window bookkeeping as dev_align leaves it. */
+__device__ __forceinline__ void fwd_move_sum(const DevSys& s, const FwdMove& m)
+{
+    const int64_t W = s.W, p = m.p;
+    double* y = s.data + p * W;
+    int kind;
+    int64_t ko;
+    uint64_t sto;
+    seq_origin(s, p, kind, ko, sto);
+    const int64_t n0 = s.n0;
+    const double o = off_of(s, p);
+    double acc = s.acc_end[p];
+    for (int64_t j = m.keep; j < W; ++j) {
+        const int64_t k = m.ns + j;
+        const double d = __ldcg(y + j);
+        double yk;
+        if (kind) {
+            acc = FQ_ADD(acc, d);
+            yk = acc;
+        }
+        else if (k < n0) {
+            acc = FQ_ADD(acc, d);
+            yk = FQ_ADD(acc, o);
+        }
+        else if (k == n0) {
+            yk = FQ_ADD(FQ_ADD(acc, o), d);
+            acc = yk;
+        }
+        else {
+            acc = FQ_ADD(acc, d);
+            yk = acc;
+        }
+        y[j] = yk;
+    }
+    s.start[p] = m.ns;
+    s.acc_end[p] = acc;
+    const int64_t li = s.margin;
+    s.cidx[p] = (int32_t)li;
+    s.gidx[p] = m.ns + li;
+    s.wc[p] = make_wc(s, y[li], y[li + 1]);
+}
+
 /* ------------------------------------------- exact integer-pipe helpers */
 
 /* Order-preserving integer key of a double: key(a) < key(b) <=> a < b for all non-NaN a, b, with

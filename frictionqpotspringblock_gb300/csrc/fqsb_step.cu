@@ -399,11 +399,6 @@ __device__ __forceinline__ void step_epilogue(const DevSys& s, StepShared& sh, i
     int tid = threadIdx.x + threadIdx.y * blockDim.x;
     int64_t bid = blockIdx.x + (int64_t)blockIdx.y * gridDim.x;
     Ctl* c = s.ctl;
-    /* without a residual tree the rest is thread 0's work: the other threads leave now instead of
-     * waiting for its atomics (their registers go back to the SM for the next CTAs) */
-    if (!tree && tid != 0) {
-        return;
-    }
     if (tid == 0) {
         if (tree) {
             s.partials[bid] = make_double2(sf, sff);
@@ -431,9 +426,7 @@ __device__ __forceinline__ void step_epilogue(const DevSys& s, StepShared& sh, i
             sh.last = (t == gridDim.x * gridDim.y - 1) ? 1 : 0;
         }
     }
-    if (tree) {
-        __syncthreads();
-    }
+    __syncthreads();
     if (!sh.last) {
         return;
     }
@@ -452,7 +445,7 @@ __device__ __forceinline__ void step_epilogue(const DevSys& s, StepShared& sh, i
         }
     }
     double2 tot = make_double2(0.0, 0.0);
-    if (tree) {
+    if (resid) {
         tot = tree_partials(s.partials, (int64_t)gridDim.x * gridDim.y, sh.red);
     }
     if (tid == 0) {
@@ -473,21 +466,6 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_line(DevSys s
 {
     __shared__ StepShared sh;
     __shared__ double sh_un[256 * PPT];
-    const int64_t N = s.N;
-    const int T = blockDim.x;
-    const int64_t base = (int64_t)blockIdx.x * T * PPT;
-    const int64_t p0 = base + (int64_t)threadIdx.x * PPT;
-    /* the cached wells do not depend on the run state: their loads are issued first, so that their
-     * latency overlaps the run-state read, the state loads and the position update */
-    double4_32a wpre[PPT];
-    if (!redo) {
-#pragma unroll
-        for (int j = 0; j < PPT; ++j) {
-            if (p0 + j < N) {
-                wpre[j] = s.wc[p0 + j];
-            }
-        }
-    }
     if (!step_prologue(s, sh, true)) {
         return;
     }
@@ -499,13 +477,6 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_line(DevSys s
         if (threadIdx.x == 0) {
             s.cta_pending[blockIdx.x] = 0;
         }
-        /* after the regeneration kernel moved windows */
-#pragma unroll
-        for (int j = 0; j < PPT; ++j) {
-            if (p0 + j < N) {
-                wpre[j] = s.wc[p0 + j];
-            }
-        }
     }
     const int cur = sh.cur;
     const bool act = (sh.flags & (RF_ACT | RF_TRUNCATE | RF_EVENT)) != 0;
@@ -514,6 +485,10 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_line(DevSys s
     const bool record = (sh.flags & RF_RECORD) != 0;
     const int64_t rec_step = record ? ((volatile Ctl*)s.ctl)->step : 0;
     const double uf = sh.uf;
+    const int64_t N = s.N;
+    const int T = blockDim.x;
+    const int64_t base = (int64_t)blockIdx.x * T * PPT;
+    const int64_t p0 = base + (int64_t)threadIdx.x * PPT;
     const double* u0 = s.u[cur];
     const double* v0 = s.v[cur];
     const double* a0 = s.a[cur];
@@ -522,6 +497,15 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_line(DevSys s
     double* a1 = s.a[cur ^ 1];
 
     double un[PPT], vr[PPT], ar[PPT];
+    /* the cached wells are loaded together with the state, so that their latency overlaps the
+     * position update and the neighbour exchange instead of following them */
+    double4_32a wpre[PPT];
+#pragma unroll
+    for (int j = 0; j < PPT; ++j) {
+        if (p0 + j < N) {
+            wpre[j] = s.wc[p0 + j];
+        }
+    }
     if (PPT == 2) {
         double2 uu = *reinterpret_cast<const double2*>(u0 + p0);
         double2 vv = *reinterpret_cast<const double2*>(v0 + p0);
@@ -789,11 +773,7 @@ __global__ void __launch_bounds__(128) k_regen(DevSys s)
     const int cur = c->cur;
     const bool act = (c->flags & (RF_ACT | RF_TRUNCATE | RF_EVENT)) != 0;
     const int n = c->n_regen;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        int64_t p = s.regen_list[k];
-        double un = u_next(s, s.u[cur], s.v[cur], s.a[cur], p);
-        int64_t gold = s.gidx[p];
-        dev_align(s, p, un);
+    auto count_move = [&](int64_t p, int64_t gold) {
         int64_t gnew = s.gidx[p];
         if (act && gnew != gold) {
             int64_t ref = s.i_n[p];
@@ -802,6 +782,49 @@ __global__ void __launch_bounds__(128) k_regen(DevSys s)
             atomicAdd((unsigned long long*)&c->s_sum, (unsigned long long)ds);
             atomicAdd((unsigned long long*)&c->a_count, (unsigned long long)da);
         }
+    };
+    if (n >= (int)(gridDim.x * blockDim.x) / 4) {
+        /* many moves: one thread per particle keeps every thread busy */
+        for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+            int64_t p = s.regen_list[k];
+            int64_t gold = s.gidx[p];
+            dev_align(s, p, u_next(s, s.u[cur], s.v[cur], s.a[cur], p));
+            count_move(p, gold);
+        }
+        return;
+    }
+    /* few moves: one CTA per particle, its threads sharing the draws (fwd_move_*); the same values */
+    __shared__ FwdMove m_sh;
+    __shared__ int ok_sh;
+    __shared__ long long gold_sh;
+    const uint64_t mv_c = pcg_advance(0ULL, (uint64_t)blockDim.x);
+    const uint64_t mv_a = pcg_advance(1ULL, (uint64_t)blockDim.x) - mv_c;
+    for (int k = blockIdx.x; k < n; k += gridDim.x) {
+        const int64_t p = s.regen_list[k];
+        if (threadIdx.x == 0) {
+            double un = u_next(s, s.u[cur], s.v[cur], s.a[cur], p);
+            gold_sh = s.gidx[p];
+            FwdMove m;
+            ok_sh = fwd_move_plan(s, p, un, m) ? 1 : 0;
+            if (ok_sh) {
+                m_sh = m;
+            }
+            else {
+                dev_align(s, p, un);
+            }
+        }
+        __syncthreads();
+        if (ok_sh) {
+            fwd_move_draws(s, m_sh, (int)threadIdx.x, (int)blockDim.x, mv_a, mv_c);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            if (ok_sh) {
+                fwd_move_sum(s, m_sh);
+            }
+            count_move(p, gold_sh);
+        }
+        __syncthreads();
     }
 }
 
@@ -1252,6 +1275,10 @@ __global__ void __launch_bounds__(256) k_run_small(DevSys s)
     __shared__ int sh_exit;
     __shared__ int sh_nan, sh_walk;
     __shared__ unsigned long long sh_ds, sh_da;
+    /* window moves of this step shared by the CTA's threads (fwd_move_*) */
+    constexpr int SMALL_MOVES = 32;
+    __shared__ FwdMove sh_moves[SMALL_MOVES];
+    __shared__ int sh_nmove;
 
     const unsigned rank = cluster.block_rank();
     const unsigned G = cluster.num_blocks();
@@ -1308,6 +1335,9 @@ __global__ void __launch_bounds__(256) k_run_small(DevSys s)
     }
     /* one particle per thread: latency bound, all fp64 on the fp64 pipe; more: throughput bound, split */
     constexpr unsigned SOFT = PPT >= 2 ? STEP_SOFT : 0u;
+    /* pcg32 stride of blockDim.x steps, x -> mv_a x + mv_c, for the shared draws of window moves */
+    const uint64_t mv_c = pcg_advance(0ULL, (uint64_t)blockDim.x);
+    const uint64_t mv_a = pcg_advance(1ULL, (uint64_t)blockDim.x) - mv_c;
     int buf = 0;
     bool first = true;
     for (;;) {
@@ -1337,6 +1367,92 @@ __global__ void __launch_bounds__(256) k_run_small(DevSys s)
         first = false;
         double rf = 0.0, rff = 0.0;
         bool nan = false;
+        /* plastic activity of a particle whose well index went from gold to gnew */
+        auto count_move = [&](int64_t p, int64_t gold, int64_t gnew) {
+            if (act && gnew != gold) {
+                int64_t ref = s.i_n[p];
+                long long ds = absll(gnew - ref) - absll(gold - ref);
+                long long da = (long long)(gnew != ref) - (long long)(gold != ref);
+                atomicAdd(&sh_ds, (unsigned long long)ds);
+                atomicAdd(&sh_da, (unsigned long long)da);
+            }
+        };
+        /* wells: a search inside the chunk window, or a window move */
+        int64_t gold[PPT];
+        bool mv[PPT];
+        bool any_mv = false;
+#pragma unroll
+        for (int j = 0; j < PPT; ++j) {
+            int64_t p = p0 + j;
+            mv[j] = false;
+            if (p >= N) {
+                continue;
+            }
+            double up = un[j];
+            double4_32a ww = w[j];
+            if (!in_well(ww.x, ww.y, up) && !non_finite(up)) {
+                gold[j] = s.gidx[p];
+                if (window_search(s, p, up, ww)) {
+                    count_move(p, gold[j], s.gidx[p]);
+                    w[j] = ww;
+                }
+                else {
+                    mv[j] = true;
+                    any_mv = true;
+                }
+            }
+        }
+        if (tid == 0) {
+            sh_nmove = 0;
+        }
+        if (__syncthreads_or(any_mv)) {
+            /* moves planned here are drawn by all threads of the CTA, then summed by their owners;
+             * the others (more than SMALL_MOVES, or not a forward move) go through dev_align */
+            int slot[PPT];
+#pragma unroll
+            for (int j = 0; j < PPT; ++j) {
+                slot[j] = -1;
+                if (mv[j]) {
+                    int k = atomicAdd(&sh_nmove, 1);
+                    if (k < SMALL_MOVES) {
+                        FwdMove m;
+                        if (fwd_move_plan(s, p0 + j, un[j], m)) {
+                            sh_moves[k] = m;
+                            slot[j] = k;
+                        }
+                        else {
+                            sh_moves[k].p = -1;
+                        }
+                    }
+                }
+            }
+            __syncthreads();
+            const int nm = sh_nmove < SMALL_MOVES ? sh_nmove : SMALL_MOVES;
+            for (int k = 0; k < nm; ++k) {
+                if (sh_moves[k].p >= 0) {
+                    fwd_move_draws(s, sh_moves[k], tid, (int)blockDim.x, mv_a, mv_c);
+                }
+            }
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < PPT; ++j) {
+                if (!mv[j]) {
+                    continue;
+                }
+                int64_t p = p0 + j;
+                if (slot[j] >= 0) {
+                    fwd_move_sum(s, sh_moves[slot[j]]);
+                }
+                else {
+                    dev_align(s, p, un[j]); /* moves the chunk window; a failed search sets walk_flag */
+                    if (((volatile Ctl*)s.ctl)->walk_flag) {
+                        sh_walk = 1;
+                    }
+                }
+                w[j] = s.wc[p];
+                count_move(p, gold[j], s.gidx[p]);
+            }
+        }
 #pragma unroll
         for (int j = 0; j < PPT; ++j) {
             int64_t p = p0 + j;
@@ -1344,26 +1460,7 @@ __global__ void __launch_bounds__(256) k_run_small(DevSys s)
                 continue;
             }
             double up = un[j];
-            double4_32a ww = w[j];
-            if (!in_well(ww.x, ww.y, up) && !non_finite(up)) {
-                int64_t gold = s.gidx[p];
-                if (!window_search(s, p, up, ww)) {
-                    dev_align(s, p, up); /* moves the chunk window; a failed search sets walk_flag */
-                    ww = s.wc[p];
-                    if (((volatile Ctl*)s.ctl)->walk_flag) {
-                        sh_walk = 1;
-                    }
-                }
-                int64_t gnew = s.gidx[p];
-                if (act && gnew != gold) {
-                    int64_t ref = s.i_n[p];
-                    long long ds = absll(gnew - ref) - absll(gold - ref);
-                    long long da = (long long)(gnew != ref) - (long long)(gold != ref);
-                    atomicAdd(&sh_ds, (unsigned long long)ds);
-                    atomicAdd(&sh_da, (unsigned long long)da);
-                }
-                w[j] = ww;
-            }
+            const double4_32a ww = w[j];
             double ff;
             double sfp = frame_pot<POT, SOFT>(s, ww, up, uf, ff);
             double fi = 0.0;
