@@ -705,27 +705,47 @@ __device__ __forceinline__ void fwd_move_sum(const DevSys& s, const FwdMove& m)
     const int64_t n0 = s.n0;
     const double o = off_of(s, p);
     double acc = s.acc_end[p];
-    for (int64_t j = m.keep; j < W; ++j) {
-        const int64_t k = m.ns + j;
-        const double d = __ldcg(y + j);
-        double yk;
-        if (kind) {
-            acc = FQ_ADD(acc, d);
-            yk = acc;
+    /* the draws are read in blocks of 16 independent loads, so that the chain of additions, not the
+     * memory latency, sets the pace */
+    constexpr int B = 16;
+    for (int64_t j0 = m.keep; j0 < W; j0 += B) {
+        double d[B];
+#pragma unroll
+        for (int i = 0; i < B; ++i) {
+            d[i] = j0 + i < W ? __ldcg(y + j0 + i) : 0.0;
         }
-        else if (k < n0) {
-            acc = FQ_ADD(acc, d);
-            yk = FQ_ADD(acc, o);
+#pragma unroll
+        for (int i = 0; i < B; ++i) {
+            const int64_t j = j0 + i;
+            if (j >= W) {
+                break;
+            }
+            const int64_t k = m.ns + j;
+            double yk;
+            if (kind) {
+                acc = FQ_ADD(acc, d[i]);
+                yk = acc;
+            }
+            else if (k < n0) {
+                acc = FQ_ADD(acc, d[i]);
+                yk = FQ_ADD(acc, o);
+            }
+            else if (k == n0) {
+                yk = FQ_ADD(FQ_ADD(acc, o), d[i]);
+                acc = yk;
+            }
+            else {
+                acc = FQ_ADD(acc, d[i]);
+                yk = acc;
+            }
+            d[i] = yk;
         }
-        else if (k == n0) {
-            yk = FQ_ADD(FQ_ADD(acc, o), d);
-            acc = yk;
+#pragma unroll
+        for (int i = 0; i < B; ++i) {
+            if (j0 + i < W) {
+                y[j0 + i] = d[i];
+            }
         }
-        else {
-            acc = FQ_ADD(acc, d);
-            yk = acc;
-        }
-        y[j] = yk;
     }
     s.start[p] = m.ns;
     s.acc_end[p] = acc;

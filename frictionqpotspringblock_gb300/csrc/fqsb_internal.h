@@ -39,6 +39,7 @@ cudaError_t build_run_graph(DevSys& s, const LineGeom& g, cudaGraphExec_t* exec)
 /* Small Line1d / Particles systems: a whole run in one launch of one thread-block cluster. */
 static const int SMALL_MAX_CTAS = 16;   /* cluster size limit (above 8 needs the non-portable opt-in) */
 static const int SMALL_RING_MAX = 1024; /* StopList windows up to this length stay in shared memory */
+static const int SMALL_THREADS_MAX = 256; /* particle threads per CTA (each CTA adds one control warp) */
 struct SmallGeom {
     int threads; /* per CTA, power of two in [32, 256] */
     int ppt;     /* particles per thread: 1, 2 or 4 */

@@ -1250,32 +1250,99 @@ cudaError_t launch_nopass_iteration(const DevSys& s, const LineGeom& g, const No
 
 /*
  * A whole run of a small Line1d / Particles system in one launch of one thread-block cluster (up to
- * 8 CTAs on 8 SMs).  For small N the graph path is bound by its per-step launch and node overhead
- * (about 20 us per time step at N = 1024, no faster than one CPU core); here the state stays in
+ * 16 CTAs on 16 SMs).  For small N the graph path is bound by its per-step launch and node overhead
+ * (about 18 us per time step at N = 1024, no faster than one CPU core); here the state stays in
  * registers for the whole run, the new positions at tile edges cross CTA boundaries through
- * distributed shared memory, and cluster barriers replace the per-step launches.  Per time step:
- *   position update -> barrier A -> wells, forces, velocities, CTA residual subtree -> barrier B ->
- *   CTA 0 sums the subtrees and runs the same stop tests as the graph path (finalize_step) ->
- *   barrier C -> every CTA reads the decision.
- * Arithmetic, the residual tree (aligned power-of-two tiles) and the finalisation are those of
- * k_step_line, and chunk windows are moved inline (dev_align, as k_regen does), so the results equal
- * the graph path's bit for bit.  Runs that record a trajectory (adjoint) use the graph path.
+ * distributed shared memory, and one cluster barrier per time step replaces the per-step launches.
+ *
+ * Every CTA has its particle threads and one control warp (the last warp).  Time step t:
+ *   position update -> cluster barrier A_t -> wells, forces, velocities, the CTA's residual subtree
+ *   and counters, published to CTA 0's slot t % 2 -> position update of step t + 1 -> A_{t+1} ...
+ * Meanwhile, after A_{t+1}, CTA 0's control warp sums step t's subtrees, applies its counters and
+ * runs the same stop tests as the graph path (finalize_ctl); its decision is read by every thread
+ * after A_{t+2}.  The decision thus comes two barriers late: when it says stop after step t, the
+ * threads have already taken step t + 1, and they restore the state from before that step (positions,
+ * velocities, accelerations, and the well and chunk window as they were) -- the step's counters were
+ * never applied.  The stop tests therefore leave the critical path, and one barrier per step remains.
+ * Arithmetic, the residual tree (aligned power-of-two tiles) and the stop tests are those of
+ * k_step_line, and chunk windows move as k_regen moves them, so the results equal the graph path's
+ * bit for bit.  Runs that record a trajectory (adjoint) use the graph path.
  */
+
+/* Named barrier 1 over the particle threads of the CTA (the control warp is not in it). */
+__device__ __forceinline__ void particle_bar(int n)
+{
+    asm volatile("bar.sync 1, %0;" ::"r"(n) : "memory");
+}
+
+/* particle_bar that also returns whether any particle thread passed a non-zero flag */
+__device__ __forceinline__ int particle_bar_or(int n, int flag)
+{
+    int r;
+    asm volatile("{\n\t.reg .pred p, q;\n\tsetp.ne.s32 p, %1, 0;\n\tbar.red.or.pred q, 1, %2, p;\n\t"
+                 "selp.s32 %0, 1, 0, q;\n\t}"
+                 : "=r"(r)
+                 : "r"(flag), "r"(n)
+                 : "memory");
+    return r;
+}
+
+/* cta_tree2 over the first nt threads of the CTA (nt a multiple of 32), with the named barrier */
+__device__ __forceinline__ double2 particle_tree2(double x, double y, double* sh, int nt)
+{
+#pragma unroll
+    for (int m = 1; m < 32; m <<= 1) {
+        double xo = __shfl_down_sync(0xffffffffu, x, m);
+        double yo = __shfl_down_sync(0xffffffffu, y, m);
+        if ((threadIdx.x & (2 * m - 1)) == 0) {
+            x = add_nospec(x, xo);
+            y = add_nospec(y, yo);
+        }
+    }
+    int nw = nt >> 5;
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    particle_bar(nt);
+    if (lane == 0) {
+        sh[wid] = x;
+        sh[32 + wid] = y;
+    }
+    particle_bar(nt);
+    if (wid == 0) {
+        double a = lane < nw ? sh[lane] : 0.0;
+        double b = lane < nw ? sh[32 + lane] : 0.0;
+#pragma unroll
+        for (int m = 1; m < 32; m <<= 1) {
+            double ao = __shfl_down_sync(0xffffffffu, a, m);
+            double bo = __shfl_down_sync(0xffffffffu, b, m);
+            if ((threadIdx.x & (2 * m - 1)) == 0) {
+                a = add_nospec(a, ao);
+                b = add_nospec(b, bo);
+            }
+        }
+        x = a;
+        y = b;
+    }
+    return make_double2(x, y);
+}
+
 template <int POT, int INTER, int PPT>
-__global__ void __launch_bounds__(256) k_run_small(DevSys s)
+__global__ void __launch_bounds__(SMALL_THREADS_MAX + 32, 1) k_run_small(DevSys s)
 {
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
-    __shared__ double sh_un[2][256 * PPT];
+    __shared__ double sh_un[2][SMALL_THREADS_MAX * PPT];
     __shared__ double red[64];
-    /* CTA 0 keeps the run-control block, the StopList window and the CTA subtrees of the residual */
+    /* CTA 0 keeps the run-control block and the StopList window, and per step parity the CTAs'
+     * residual subtrees and counters, and the stop decision */
     __shared__ Ctl sc;
     __shared__ double sring[SMALL_RING_MAX];
-    __shared__ double2 spart[SMALL_MAX_CTAS];
-    __shared__ int sh_exit;
+    __shared__ double2 spart[2][SMALL_MAX_CTAS];
+    __shared__ unsigned long long sl_ds[2], sl_da[2];
+    __shared__ int sl_nan[2], sl_walk[2], sl_stop[2];
+    /* this CTA's counters of the current step */
     __shared__ int sh_nan, sh_walk;
     __shared__ unsigned long long sh_ds, sh_da;
-    /* window moves of this step shared by the CTA's threads (fwd_move_*) */
+    /* window moves of this step shared by the CTA's particle threads (fwd_move_*) */
     constexpr int SMALL_MOVES = 32;
     __shared__ FwdMove sh_moves[SMALL_MOVES];
     __shared__ int sh_nmove;
@@ -1283,8 +1350,10 @@ __global__ void __launch_bounds__(256) k_run_small(DevSys s)
     const unsigned rank = cluster.block_rank();
     const unsigned G = cluster.num_blocks();
     const int tid = threadIdx.x;
+    const int pt = (int)blockDim.x - 32; /* particle threads; the last warp is the control warp */
+    const bool ctrl = tid >= pt;
     const int64_t N = s.N;
-    const int64_t tile = (int64_t)blockDim.x * PPT;
+    const int64_t tile = (int64_t)pt * PPT;
     const int64_t base = (int64_t)rank * tile;
     const int64_t p0 = base + (int64_t)tid * PPT;
     const Ctl* gc = s.ctl;
@@ -1302,6 +1371,13 @@ __global__ void __launch_bounds__(256) k_run_small(DevSys s)
         for (int64_t i = tid; i < nring; i += blockDim.x) {
             sring[i] = s.ring[i];
         }
+        if (tid < 2) {
+            sl_ds[tid] = 0ull;
+            sl_da[tid] = 0ull;
+            sl_nan[tid] = 0;
+            sl_walk[tid] = 0;
+            sl_stop[tid] = 0;
+        }
     }
 
     /* ring neighbours of the tile's first and last particle: (CTA rank, index in its tile) */
@@ -1314,15 +1390,22 @@ __global__ void __launch_bounds__(256) k_run_small(DevSys s)
     const double* right[2] = {cluster.map_shared_rank(&sh_un[0][0], (unsigned)(pr / tile)),
                               cluster.map_shared_rank(&sh_un[1][0], (unsigned)(pr / tile))};
     Ctl* sc0 = cluster.map_shared_rank(&sc, 0);
-    double2* spart0 = cluster.map_shared_rank(&spart[0], 0);
-    const int* exit0 = cluster.map_shared_rank(&sh_exit, 0);
+    double2* spart0 = cluster.map_shared_rank(&spart[0][0], 0);
+    unsigned long long* sl_ds0 = cluster.map_shared_rank(&sl_ds[0], 0);
+    unsigned long long* sl_da0 = cluster.map_shared_rank(&sl_da[0], 0);
+    int* sl_nan0 = cluster.map_shared_rank(&sl_nan[0], 0);
+    int* sl_walk0 = cluster.map_shared_rank(&sl_walk[0], 0);
+    const int* sl_stop0 = cluster.map_shared_rank(&sl_stop[0], 0);
 
     double u[PPT], v[PPT], a[PPT];
     double4_32a w[PPT];
+    /* the state before the latest step, kept for the rollback of a step taken after the stop */
+    double pu[PPT], pv[PPT], pa[PPT];
+    int64_t pstart[PPT];
 #pragma unroll
     for (int j = 0; j < PPT; ++j) {
         int64_t p = p0 + j;
-        if (p < N) {
+        if (!ctrl && p < N) {
             u[j] = s.u[cur][p];
             v[j] = s.v[cur][p];
             a[j] = s.a[cur][p];
@@ -1332,39 +1415,118 @@ __global__ void __launch_bounds__(256) k_run_small(DevSys s)
             u[j] = v[j] = a[j] = 0.0;
             w[j] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
         }
+        pu[j] = u[j];
+        pv[j] = v[j];
+        pa[j] = a[j];
+        pstart[j] = 0;
     }
     /* one particle per thread: latency bound, all fp64 on the fp64 pipe; more: throughput bound, split */
     constexpr unsigned SOFT = PPT >= 2 ? STEP_SOFT : 0u;
-    /* pcg32 stride of blockDim.x steps, x -> mv_a x + mv_c, for the shared draws of window moves */
-    const uint64_t mv_c = pcg_advance(0ULL, (uint64_t)blockDim.x);
-    const uint64_t mv_a = pcg_advance(1ULL, (uint64_t)blockDim.x) - mv_c;
+    /* pcg32 stride of pt steps, x -> mv_a x + mv_c, for the shared draws of window moves */
+    const uint64_t mv_c = pcg_advance(0ULL, (uint64_t)pt);
+    const uint64_t mv_a = pcg_advance(1ULL, (uint64_t)pt) - mv_c;
     int buf = 0;
-    bool first = true;
-    for (;;) {
-        const double uf_prev = uf;
-        if (flags & RF_FLOW) {
-            uf = FQ_ADD(uf, vdt);
-        }
+    double uf_prev = uf;
+    for (int64_t t = 0;; ++t) {
+        const double uf_t = (flags & RF_FLOW) ? FQ_ADD(uf, vdt) : uf;
         double un[PPT];
+        if (!ctrl) {
 #pragma unroll
-        for (int j = 0; j < PPT; ++j) {
-            un[j] = S_ADD(3, S_ADD(2, u[j], S_MUL(0, s.dt, v[j])), S_MUL(1, s.hdt2, a[j]));
-            sh_un[buf][tid * PPT + j] = un[j];
+            for (int j = 0; j < PPT; ++j) {
+                un[j] = S_ADD(3, S_ADD(2, u[j], S_MUL(0, s.dt, v[j])), S_MUL(1, s.hdt2, a[j]));
+                sh_un[buf][tid * PPT + j] = un[j];
+            }
         }
         if (tid == 0) {
             sh_ds = 0ull;
             sh_da = 0ull;
             sh_nan = 0;
             sh_walk = 0;
+            sh_nmove = 0;
         }
-        /* A: every tile's new positions, and CTA 0's decision on the previous step (at the start: its
-         * control block).  On a stop the positions just computed are dropped. */
+        /* A_t: every tile's new positions, the subtrees and counters of step t - 1, and the decision
+         * after step t - 2 (slot t % 2) */
         cluster.sync();
-        if (!first && *exit0) {
-            uf = uf_prev;
+        if (t >= 2 && sl_stop0[t & 1]) {
+            /* stopped after step t - 2: restore the state before step t - 1 */
+            if (!ctrl) {
+#pragma unroll
+                for (int j = 0; j < PPT; ++j) {
+                    int64_t p = p0 + j;
+                    u[j] = pu[j];
+                    v[j] = pv[j];
+                    a[j] = pa[j];
+                    if (p >= N) {
+                        continue;
+                    }
+                    bool placed = false;
+                    if (s.start[p] != pstart[j]) {
+                        /* the window moved in the step taken after the stop: put it back */
+                        double acc;
+                        seq_fill(s, p, pstart[j], s.W, s.data + p * s.W, &acc);
+                        s.start[p] = pstart[j];
+                        s.acc_end[p] = acc;
+                        placed = true;
+                    }
+                    /* the well of the restored position (index, cached well) in the restored window */
+                    double4_32a ww = s.wc[p];
+                    if ((placed || !in_well(ww.x, ww.y, u[j])) && !non_finite(u[j]) &&
+                        !window_search(s, p, u[j], ww)) {
+                        dev_align(s, p, u[j]);
+                    }
+                }
+            }
             break;
         }
-        first = false;
+        const double uf_last = uf_prev; /* u_frame of step t - 1, for its stop tests */
+        uf_prev = uf_t;
+        uf = uf_t;
+        if (ctrl) {
+            if (rank == 0 && t >= 1) {
+                /* the decision after step t - 1 */
+                const int q = (int)((t - 1) & 1);
+                const int lane = tid - pt;
+                double tx = 0.0, ty = 0.0;
+                if (resid) {
+                    /* the canonical tree over the CTA subtrees, zero padded (as tree_partials): G <= 32 */
+                    double x = 0.0, y = 0.0;
+                    if ((unsigned)lane < G) {
+                        x = spart[q][lane].x;
+                        y = spart[q][lane].y;
+                    }
+                    tx = warp_tree(x);
+                    ty = warp_tree(y);
+                }
+                if (lane == 0) {
+                    sc.s_sum = (long long)((unsigned long long)sc.s_sum + sl_ds[q]);
+                    sc.a_count = (long long)((unsigned long long)sc.a_count + sl_da[q]);
+                    if (sl_nan[q]) {
+                        sc.nan_flag = 1;
+                    }
+                    if (sl_walk[q]) {
+                        sc.walk_flag = 1;
+                    }
+                    sl_ds[q] = 0ull;
+                    sl_da[q] = 0ull;
+                    sl_nan[q] = 0;
+                    sl_walk[q] = 0;
+                    finalize_ctl(&sc, sring, uf_last, tx, ty);
+                    sl_stop[q] = (sc.done || sc.error || (globaltimer() - sc.launch_t0) >= sc.budget_ns) ? 1 : 0;
+                }
+            }
+            buf ^= 1;
+            continue;
+        }
+        /* the particle threads take step t */
+#pragma unroll
+        for (int j = 0; j < PPT; ++j) {
+            pu[j] = u[j];
+            pv[j] = v[j];
+            pa[j] = a[j];
+            if (p0 + j < N) {
+                pstart[j] = s.start[p0 + j];
+            }
+        }
         double rf = 0.0, rff = 0.0;
         bool nan = false;
         /* plastic activity of a particle whose well index went from gold to gnew */
@@ -1402,12 +1564,9 @@ __global__ void __launch_bounds__(256) k_run_small(DevSys s)
                 }
             }
         }
-        if (tid == 0) {
-            sh_nmove = 0;
-        }
-        if (__syncthreads_or(any_mv)) {
-            /* moves planned here are drawn by all threads of the CTA, then summed by their owners;
-             * the others (more than SMALL_MOVES, or not a forward move) go through dev_align */
+        if (particle_bar_or(pt, any_mv ? 1 : 0)) {
+            /* moves planned here are drawn by all particle threads of the CTA, then summed by their
+             * owners; the others (more than SMALL_MOVES, or not a forward move) go through dev_align */
             int slot[PPT];
 #pragma unroll
             for (int j = 0; j < PPT; ++j) {
@@ -1426,14 +1585,14 @@ __global__ void __launch_bounds__(256) k_run_small(DevSys s)
                     }
                 }
             }
-            __syncthreads();
+            particle_bar(pt);
             const int nm = sh_nmove < SMALL_MOVES ? sh_nmove : SMALL_MOVES;
             for (int k = 0; k < nm; ++k) {
                 if (sh_moves[k].p >= 0) {
-                    fwd_move_draws(s, sh_moves[k], tid, (int)blockDim.x, mv_a, mv_c);
+                    fwd_move_draws(s, sh_moves[k], tid, pt, mv_a, mv_c);
                 }
             }
-            __syncthreads();
+            particle_bar(pt);
 #pragma unroll
             for (int j = 0; j < PPT; ++j) {
                 if (!mv[j]) {
@@ -1494,54 +1653,40 @@ __global__ void __launch_bounds__(256) k_run_small(DevSys s)
         }
         double2 sfs = make_double2(0.0, 0.0);
         if (resid) {
-            sfs = cta_tree2(rf, rff, red);
+            sfs = particle_tree2(rf, rff, red, pt);
         }
-        __syncthreads();
+        particle_bar(pt);
         if (tid == 0) {
+            /* publish step t to CTA 0's slot t % 2 */
+            const int q = (int)(t & 1);
             if (resid) {
-                spart0[rank] = sfs;
+                spart0[q * SMALL_MAX_CTAS + rank] = sfs;
             }
             if (sh_ds) {
-                atomicAdd((unsigned long long*)&sc0->s_sum, sh_ds);
+                atomicAdd(sl_ds0 + q, sh_ds);
             }
             if (sh_da) {
-                atomicAdd((unsigned long long*)&sc0->a_count, sh_da);
+                atomicAdd(sl_da0 + q, sh_da);
             }
             if (sh_nan) {
-                atomicOr(&sc0->nan_flag, 1);
+                atomicOr(sl_nan0 + q, 1);
             }
             if (sh_walk) {
-                atomicOr(&sc0->walk_flag, 1);
-            }
-        }
-        cluster.sync(); /* B: every tile's residual subtree and counters */
-        if (rank == 0 && tid < 32) {
-            double tx = 0.0, ty = 0.0;
-            if (resid) {
-                /* the canonical tree over the CTA subtrees, zero padded (as tree_partials): G <= 32 */
-                double x = 0.0, y = 0.0;
-                if ((unsigned)tid < G) {
-                    x = spart[tid].x;
-                    y = spart[tid].y;
-                }
-                tx = warp_tree(x);
-                ty = warp_tree(y);
-            }
-            if (tid == 0) {
-                finalize_ctl(&sc, sring, uf, tx, ty);
-                sh_exit = (sc.done || sc.error || (globaltimer() - sc.launch_t0) >= sc.budget_ns) ? 1 : 0;
+                atomicOr(sl_walk0 + q, 1);
             }
         }
         buf ^= 1;
     }
     cur = sc0->cur;
+    if (!ctrl) {
 #pragma unroll
-    for (int j = 0; j < PPT; ++j) {
-        int64_t p = p0 + j;
-        if (p < N) {
-            s.u[cur][p] = u[j];
-            s.v[cur][p] = v[j];
-            s.a[cur][p] = a[j];
+        for (int j = 0; j < PPT; ++j) {
+            int64_t p = p0 + j;
+            if (p < N) {
+                s.u[cur][p] = u[j];
+                s.v[cur][p] = v[j];
+                s.a[cur][p] = a[j];
+            }
         }
     }
     if (rank == 0) {
@@ -1604,7 +1749,7 @@ static void small_launch_config(const SmallGeom& g, cudaStream_t st, cudaLaunchC
 {
     cfg = {};
     cfg.gridDim = dim3((unsigned)g.ctas);
-    cfg.blockDim = dim3((unsigned)g.threads);
+    cfg.blockDim = dim3((unsigned)g.threads + 32u); /* particle threads and the control warp */
     cfg.dynamicSmemBytes = 0;
     cfg.stream = st;
     attr[0].id = cudaLaunchAttributeClusterDimension;
