@@ -235,7 +235,8 @@ def bench_line2d(fqsb, full=False):
     """Line2d System_Cuspy_Laplace on a 2048 x 2048 periodic grid: m = 1, eta = 0.2, mu = 1, k = 1,
     k_frame = 1/2048^2, dt = 0.1, Weibull(2,1)+1e-5 from pcg32 seed 2, 500 yield positions per site;
     cycles of eventDrivenStep(1e-5, kick=False), eventDrivenStep(1e-5, kick=True), minimise(tol=1e-5)
-    (20 with --full, else 1 warm-up + 2 timed); then a regeneration sweep: u += 600 and back (every
+    (20 with --full, else 1 warm-up + 2 timed); flowSteps(200, v_frame = 1e-3) for the dynamics without
+    the residual; then a regeneration sweep: u += 600 and back (every
     site crosses ~680 wells, so every chunk window is regenerated from its pcg32 stream, forward then
     backward)."""
     side = 2048
@@ -265,6 +266,12 @@ def bench_line2d(fqsb, full=False):
     ps = n * tot_steps / tot_t
     out.update(seconds=tot_t, time_steps=tot_steps, particle_steps_per_s=ps,
                hbm_frac_64B=BYTES_PER_PARTICLE_STEP * ps / 1e9 / peaks()[0])
+    # dynamics without the residual: flowSteps(200) with the frame moving 1e-4 per step
+    s.flowSteps(20, V_FRAME)
+    t0 = time.perf_counter()
+    s.flowSteps(200, V_FRAME)
+    tf = time.perf_counter() - t0
+    out["flow"] = {"steps": 200, "seconds": tf, "particle_steps_per_s": n * 200 / tf}
     u = s.u
     t0 = time.perf_counter()
     s.u = u + 600.0

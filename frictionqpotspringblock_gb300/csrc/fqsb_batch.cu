@@ -63,6 +63,8 @@ struct BatchRun {
     int32_t n_pending_tiles, n_regen, active, walk_flag;
     uint64_t launch_t0, budget_ns;
     int64_t launch_iters, iters;
+    int32_t n_active_tiles; /* entries of BatchDev::active_tiles: the tiles of unfinished realisations */
+    int32_t rebuild;        /* a realisation finished this iteration: rebuild the list at its end */
 };
 
 struct BatchDev {
@@ -70,7 +72,8 @@ struct BatchDev {
     Inst* inst;
     BatchRun* run;
     const int32_t* tile_inst;
-    int64_t ntiles;
+    int32_t* active_tiles; /* tile of CTA k of a pass, k < BatchRun::n_active_tiles */
+    int64_t ntiles, ninst;
     int tile, ppt;
     double2* partials;
     int32_t* tile_pending;
@@ -88,7 +91,7 @@ __device__ __forceinline__ uint64_t gtimer()
 }
 
 struct BShared {
-    int skip, phase, cur, last_inst, last_glob, pending, nan;
+    int skip, phase, cur, last_inst, last_glob, pending, nan, nact, tile;
     double uf, du_p;
     unsigned long long ds;
     unsigned long long mkey;
@@ -234,6 +237,52 @@ __device__ void inst_finalize(const BatchDev& b, Inst* I, int j, double2 tot)
     if (done) {
         I->phase = PH_DONE;
         atomicSub(&R->active, 1);
+        R->rebuild = 1;
+    }
+    __threadfence();
+}
+
+/*
+ * The list of tiles that still have work: the tiles of every unfinished realisation, in realisation
+ * order (a realisation's tiles stay consecutive, so its tile tickets and partials are unchanged).
+ * Run by all threads of the CTA that ends the iteration; each thread takes a contiguous run of
+ * realisations, an exclusive scan over the threads places their tiles.
+ */
+__device__ void rebuild_active_tiles(const BatchDev& b)
+{
+    __shared__ int64_t scan[256];
+    const int T = blockDim.x;
+    const int64_t ninst = b.ninst;
+    const int64_t per = (ninst + T - 1) / T;
+    const int64_t j0 = (int64_t)threadIdx.x * per, j1 = j0 + per < ninst ? j0 + per : ninst;
+    int64_t cnt = 0;
+    for (int64_t j = j0; j < j1; ++j) {
+        const volatile Inst* I = b.inst + j;
+        if (I->phase != PH_DONE) {
+            cnt += I->ntiles;
+        }
+    }
+    scan[threadIdx.x] = cnt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int64_t acc = 0;
+        for (int k = 0; k < T; ++k) {
+            int64_t c = scan[k];
+            scan[k] = acc;
+            acc += c;
+        }
+        b.run->n_active_tiles = (int32_t)acc;
+        b.run->rebuild = 0;
+    }
+    __syncthreads();
+    int64_t o = scan[threadIdx.x];
+    for (int64_t j = j0; j < j1; ++j) {
+        const volatile Inst* I = b.inst + j;
+        if (I->phase != PH_DONE) {
+            for (int64_t q = 0; q < I->ntiles; ++q) {
+                b.active_tiles[o++] = (int32_t)(I->tile0 + q);
+            }
+        }
     }
     __threadfence();
 }
@@ -274,7 +323,16 @@ __global__ void __launch_bounds__(256, 4) k_batch(BatchDev b, int redo)
 {
     __shared__ BShared sh;
     __shared__ double sh_un[256 * PPT];
-    const int64_t t = blockIdx.x;
+    if (threadIdx.x == 0) {
+        /* CTA k takes the k-th tile of an unfinished realisation; the others have nothing to do */
+        sh.nact = ((volatile BatchRun*)b.run)->n_active_tiles;
+        sh.tile = (int)blockIdx.x < sh.nact ? b.active_tiles[blockIdx.x] : -1;
+    }
+    __syncthreads();
+    if (sh.tile < 0) {
+        return;
+    }
+    const int64_t t = sh.tile;
     const int j = b.tile_inst[t];
     Inst* I = b.inst + j;
     const DevSys& s = b.d;
@@ -576,10 +634,18 @@ __global__ void __launch_bounds__(256, 4) k_batch(BatchDev b, int redo)
         }
         else {
             unsigned k = atomicAdd(&b.run->ticket, 1u);
-            sh.last_glob = k == (unsigned)gridDim.x - 1u;
+            sh.last_glob = k == (unsigned)sh.nact - 1u;
         }
-        if (sh.last_glob) {
-            __threadfence();
+    }
+    __syncthreads();
+    if (sh.last_glob) {
+        __threadfence();
+        BatchRun* R = b.run;
+        const bool iteration_end = redo || R->n_pending_tiles == 0;
+        if (iteration_end && R->rebuild) {
+            rebuild_active_tiles(b);
+        }
+        if (threadIdx.x == 0) {
             batch_iteration_end(b, redo != 0);
         }
     }
@@ -975,6 +1041,8 @@ extern "C" int fqsb_batch_create(const fqsb_batch_config* c, fqsb_batch** out)
     b.tile_inst = ti;
     BA(b.partials, (size_t)b.ntiles);
     BA(b.tile_pending, (size_t)b.ntiles);
+    BA(b.active_tiles, (size_t)b.ntiles);
+    b.ninst = h->ninst;
     BA(b.regen_list, N);
     int64_t* dvalid;
     BA(dvalid, N);
@@ -1111,6 +1179,16 @@ extern "C" int fqsb_batch_quasistatic(fqsb_batch* h, int64_t ncycles, double eps
     R.max_iter = (int64_t)max_iter;
     R.active = (int32_t)h->ninst;
     R.budget_ns = 200ull * 1000ull * 1000ull;
+    /* every realisation starts the protocol: all tiles are active */
+    R.n_active_tiles = (int32_t)b.ntiles;
+    R.rebuild = 0;
+    {
+        std::vector<int32_t> all((size_t)b.ntiles);
+        for (size_t k = 0; k < all.size(); ++k) {
+            all[k] = (int32_t)k;
+        }
+        QCU(cudaMemcpy(b.active_tiles, all.data(), sizeof(int32_t) * all.size(), cudaMemcpyHostToDevice));
+    }
     QCU(cudaMemcpyAsync(b.run, &R, sizeof(R), cudaMemcpyHostToDevice, h->stream));
     for (;;) {
         QCU(cudaGraphLaunch(h->graph, h->stream));

@@ -266,7 +266,7 @@ __device__ __forceinline__ double par_or(const DevSys& s, int i, double def)
 }
 
 /* prrng distribution transform of one draw; same expressions and order as the oracle */
-static __device__ __noinline__ double dev_transform(const DevSys& s, uint32_t r32)
+__device__ __forceinline__ double dev_transform_inl(const DevSys& s, uint32_t r32)
 {
     double r = FQ_MUL((double)r32, 0x1p-32);
     switch (s.dist) {
@@ -287,6 +287,12 @@ static __device__ __noinline__ double dev_transform(const DevSys& s, uint32_t r3
         default:
             return __longlong_as_double(0x7ff8000000000000LL);
     }
+}
+
+/* out of line where it is called in a loop (keeps the callers' registers low) */
+static __device__ __noinline__ double dev_transform(const DevSys& s, uint32_t r32)
+{
+    return dev_transform_inl(s, r32);
 }
 
 __device__ __forceinline__ double dev_draw(const DevSys& s, uint64_t st)
@@ -680,15 +686,26 @@ __device__ __forceinline__ bool fwd_move_plan(const DevSys& s, int64_t p, double
 /* Draws of one planned move: thread `lane` of `nlanes` writes the draws of window slots
  * keep + lane, keep + lane + nlanes, ... (one jump-ahead, then strides of nlanes steps: the
  * stride map x -> a x + c with c = advance(0, nlanes), a = advance(1, nlanes) - c). */
-__device__ __forceinline__ void fwd_move_draws(const DevSys& s, const FwdMove& m, int lane, int nlanes, uint64_t sa,
-                                               uint64_t sc)
+static __device__ __noinline__ void fwd_move_draws(const DevSys& s, const FwdMove& m, int lane, int nlanes,
+                                                   uint64_t sa, uint64_t sc)
 {
     const int64_t W = s.W;
     double* y = s.data + m.p * W;
-    uint64_t st = pcg_advance(m.st_first, (uint64_t)lane);
-    for (int64_t j = m.keep + lane; j < W; j += nlanes) {
-        y[j] = dev_draw(s, st);
-        st = sa * st + sc;
+    /* two draws per iteration (slots j and j + nlanes), inlined, so that their long dependency chains
+     * overlap; stride 2 nlanes: x -> sa2 x + sc2 */
+    const uint64_t sa2 = sa * sa, sc2 = sa * sc + sc;
+    uint64_t st0 = pcg_advance(m.st_first, (uint64_t)lane);
+    uint64_t st1 = sa * st0 + sc;
+    const bool delta = s.dist == DIST_DELTA;
+    for (int64_t j = m.keep + lane; j < W; j += 2 * (int64_t)nlanes) {
+        const double d0 = dev_transform_inl(s, delta ? 0u : pcg_output(st0));
+        const double d1 = dev_transform_inl(s, delta ? 0u : pcg_output(st1));
+        y[j] = d0;
+        if (j + nlanes < W) {
+            y[j + nlanes] = d1;
+        }
+        st0 = sa2 * st0 + sc2;
+        st1 = sa2 * st1 + sc2;
     }
 }
 
