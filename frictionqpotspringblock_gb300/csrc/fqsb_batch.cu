@@ -27,6 +27,7 @@
 #include <climits>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -81,6 +82,7 @@ struct BatchDev {
     double *out_uframe, *out_fframe;
     int64_t *out_S, *out_inc;
     unsigned long long h_while, h_if;
+    int in_graph; /* 0: the host launches each pass (FQSB_NO_GRAPH=1 at creation), no conditionals to set */
 };
 
 __device__ __forceinline__ uint64_t gtimer()
@@ -293,11 +295,15 @@ __device__ void batch_iteration_end(const BatchDev& b, bool redo)
     BatchRun* R = b.run;
     if (!redo && R->n_pending_tiles > 0) {
         R->ticket = 0;
-        cudaGraphSetConditional((cudaGraphConditionalHandle)b.h_if, 1u);
+        if (b.in_graph) {
+            cudaGraphSetConditional((cudaGraphConditionalHandle)b.h_if, 1u);
+        }
         return;
     }
     if (!redo) {
-        cudaGraphSetConditional((cudaGraphConditionalHandle)b.h_if, 0u);
+        if (b.in_graph) {
+            cudaGraphSetConditional((cudaGraphConditionalHandle)b.h_if, 0u);
+        }
     }
     R->ticket = 0;
     R->ticket_redo = 0;
@@ -311,7 +317,9 @@ __device__ void batch_iteration_end(const BatchDev& b, bool redo)
     R->iters += 1;
     bool more = R->active > 0 && R->walk_flag == 0 && (now - R->launch_t0) < R->budget_ns;
     __threadfence();
-    cudaGraphSetConditional((cudaGraphConditionalHandle)b.h_while, more ? 1u : 0u);
+    if (b.in_graph) {
+        cudaGraphSetConditional((cudaGraphConditionalHandle)b.h_while, more ? 1u : 0u);
+    }
 }
 
 /*
@@ -324,9 +332,11 @@ __global__ void __launch_bounds__(256, 4) k_batch(BatchDev b, int redo)
     __shared__ BShared sh;
     __shared__ double sh_un[256 * PPT];
     if (threadIdx.x == 0) {
-        /* CTA k takes the k-th tile of an unfinished realisation; the others have nothing to do */
+        /* CTA k takes the k-th tile of an unfinished realisation; the others have nothing to do.  While
+         * no realisation has finished the list is the identity (no second dependent load). */
         sh.nact = ((volatile BatchRun*)b.run)->n_active_tiles;
-        sh.tile = (int)blockIdx.x < sh.nact ? b.active_tiles[blockIdx.x] : -1;
+        sh.tile = sh.nact == (int)b.ntiles ? (int)blockIdx.x
+                                            : ((int)blockIdx.x < sh.nact ? b.active_tiles[blockIdx.x] : -1);
     }
     __syncthreads();
     if (sh.tile < 0) {
@@ -775,6 +785,7 @@ static cudaError_t build_batch_graph(BatchDev& b, int threads, cudaGraphExec_t* 
     BG(cudaGraphConditionalHandleCreate(&hi, body, 0, cudaGraphCondAssignDefault));
     b.h_while = hw;
     b.h_if = hi;
+    b.in_graph = 1;
     void* fk = b.ppt == 2 ? (void*)k_batch<2> : (void*)k_batch<1>;
     int pass1 = 0, pass2 = 1;
     void* a1[] = {(void*)&b, (void*)&pass1};
@@ -804,6 +815,7 @@ struct fqsb_batch {
     std::vector<double> kframe;
     cudaStream_t stream;
     bool own_stream;
+    bool no_graph; /* FQSB_NO_GRAPH=1 at creation: passes launched one by one (for profilers) */
     cudaGraphExec_t graph;
     std::string err;
     std::vector<void*> allocs;
@@ -912,6 +924,10 @@ extern "C" int fqsb_batch_create(const fqsb_batch_config* c, fqsb_batch** out)
     }
     fqsb_batch* h = new fqsb_batch();
     h->graph = nullptr;
+    {
+        const char* ng = getenv("FQSB_NO_GRAPH");
+        h->no_graph = ng && ng[0] == '1';
+    }
     h->ninst = c->n_instances;
     h->nchunk = c->nchunk;
     h->window = c->window;
@@ -1190,15 +1206,41 @@ extern "C" int fqsb_batch_quasistatic(fqsb_batch* h, int64_t ncycles, double eps
         QCU(cudaMemcpy(b.active_tiles, all.data(), sizeof(int32_t) * all.size(), cudaMemcpyHostToDevice));
     }
     QCU(cudaMemcpyAsync(b.run, &R, sizeof(R), cudaMemcpyHostToDevice, h->stream));
-    for (;;) {
-        QCU(cudaGraphLaunch(h->graph, h->stream));
-        QCU(cudaMemcpyAsync(&R, b.run, sizeof(R), cudaMemcpyDeviceToHost, h->stream));
-        QCU(cudaStreamSynchronize(h->stream));
-        if (R.active <= 0 || R.walk_flag) {
-            break;
+    if (h->no_graph) {
+        /* each pass launched by the host: pass 1, and the regeneration branch when tiles are pending */
+        BatchDev bh = b;
+        bh.in_graph = 0;
+        void* fk = b.ppt == 2 ? (void*)k_batch<2> : (void*)k_batch<1>;
+        int pass1 = 0, pass2 = 1;
+        void* a1[] = {(void*)&bh, (void*)&pass1};
+        void* a2[] = {(void*)&bh, (void*)&pass2};
+        void* ar[] = {(void*)&bh};
+        for (;;) {
+            QCU(cudaLaunchKernel(fk, dim3((unsigned)b.ntiles), dim3((unsigned)h->threads), a1, 0, h->stream));
+            QCU(cudaMemcpyAsync(&R, b.run, sizeof(R), cudaMemcpyDeviceToHost, h->stream));
+            QCU(cudaStreamSynchronize(h->stream));
+            if (R.n_pending_tiles > 0) {
+                QCU(cudaLaunchKernel((void*)k_batch_regen, dim3(4 * 152), dim3(128), ar, 0, h->stream));
+                QCU(cudaLaunchKernel(fk, dim3((unsigned)b.ntiles), dim3((unsigned)h->threads), a2, 0, h->stream));
+                QCU(cudaMemcpyAsync(&R, b.run, sizeof(R), cudaMemcpyDeviceToHost, h->stream));
+                QCU(cudaStreamSynchronize(h->stream));
+            }
+            if (R.active <= 0 || R.walk_flag) {
+                break;
+            }
         }
-        int64_t zero = 0;
-        QCU(cudaMemcpyAsync(&b.run->launch_iters, &zero, sizeof(zero), cudaMemcpyHostToDevice, h->stream));
+    }
+    else {
+        for (;;) {
+            QCU(cudaGraphLaunch(h->graph, h->stream));
+            QCU(cudaMemcpyAsync(&R, b.run, sizeof(R), cudaMemcpyDeviceToHost, h->stream));
+            QCU(cudaStreamSynchronize(h->stream));
+            if (R.active <= 0 || R.walk_flag) {
+                break;
+            }
+            int64_t zero = 0;
+            QCU(cudaMemcpyAsync(&b.run->launch_iters, &zero, sizeof(zero), cudaMemcpyHostToDevice, h->stream));
+        }
     }
     QCU(cudaMemcpy(u_frame_out, du, sizeof(double) * nout, cudaMemcpyDeviceToHost));
     QCU(cudaMemcpy(f_frame_out, df, sizeof(double) * nout, cudaMemcpyDeviceToHost));

@@ -1564,9 +1564,10 @@ __global__ void __launch_bounds__(SMALL_THREADS_MAX + 32, 1) k_run_small(DevSys 
                 }
             }
         }
-        if (particle_bar_or(pt, any_mv ? 1 : 0)) {
-            /* moves planned here are drawn by all particle threads of the CTA, then summed by their
-             * owners; the others (more than SMALL_MOVES, or not a forward move) go through dev_align */
+        /* window moves, in rounds of up to SMALL_MOVES: planned by their owners, drawn by all particle
+         * threads of the CTA, summed by their owners; moves that are not forward moves go through
+         * dev_align */
+        while (particle_bar_or(pt, any_mv ? 1 : 0)) {
             int slot[PPT];
 #pragma unroll
             for (int j = 0; j < PPT; ++j) {
@@ -1575,9 +1576,9 @@ __global__ void __launch_bounds__(SMALL_THREADS_MAX + 32, 1) k_run_small(DevSys 
                     int k = atomicAdd(&sh_nmove, 1);
                     if (k < SMALL_MOVES) {
                         FwdMove m;
+                        slot[j] = k;
                         if (fwd_move_plan(s, p0 + j, un[j], m)) {
                             sh_moves[k] = m;
-                            slot[j] = k;
                         }
                         else {
                             sh_moves[k].p = -1;
@@ -1593,13 +1594,18 @@ __global__ void __launch_bounds__(SMALL_THREADS_MAX + 32, 1) k_run_small(DevSys 
                 }
             }
             particle_bar(pt);
+            any_mv = false;
 #pragma unroll
             for (int j = 0; j < PPT; ++j) {
                 if (!mv[j]) {
                     continue;
                 }
+                if (slot[j] < 0) {
+                    any_mv = true; /* a later round */
+                    continue;
+                }
                 int64_t p = p0 + j;
-                if (slot[j] >= 0) {
+                if (sh_moves[slot[j]].p >= 0) {
                     fwd_move_sum(s, sh_moves[slot[j]]);
                 }
                 else {
@@ -1608,8 +1614,13 @@ __global__ void __launch_bounds__(SMALL_THREADS_MAX + 32, 1) k_run_small(DevSys 
                         sh_walk = 1;
                     }
                 }
+                mv[j] = false;
                 w[j] = s.wc[p];
                 count_move(p, gold[j], s.gidx[p]);
+            }
+            particle_bar(pt);
+            if (tid == 0) {
+                sh_nmove = 0;
             }
         }
 #pragma unroll

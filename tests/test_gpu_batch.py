@@ -89,3 +89,20 @@ def test_autotune_picks_a_candidate(tmp_path, monkeypatch):
     best = autotune.choose_tile(sizes, make, sample=16, cycles=1)
     assert tuple(best) in autotune.CANDIDATES
     assert autotune.choose_tile(sizes, make) == tuple(best)  # cached
+
+
+def test_batch_host_driven(monkeypatch):
+    """FQSB_NO_GRAPH=1 at creation: the batch's passes are launched one by one from the host (the form
+    profilers can see); results equal the graph form's bit for bit, window moves included."""
+    sizes = B.log_uniform_sizes(24, 8, 1024, seed=3)
+    seeds = 1000 + np.arange(len(sizes))
+    out = []
+    for ng in ("0", "1"):
+        monkeypatch.setenv("FQSB_NO_GRAPH", ng)
+        b = B.Line1d_System_Cuspy_Laplace(sizes, seeds, 1.0 / sizes, nchunk=100, window=34, **COMMON)
+        monkeypatch.delenv("FQSB_NO_GRAPH")
+        out.append(b.quasistatic(6, 0.3, max_iter=2000000))
+        out[-1]["u"] = np.concatenate([b.field(j, "u") for j in range(len(sizes))])
+        del b
+    for k in ("u_frame", "f_frame", "S", "inc", "status", "u"):
+        assert np.array_equal(out[0][k], out[1][k]), k
