@@ -34,7 +34,10 @@ int64_t step_ctas(const DevSys& s, const LineGeom& g);
 
 /* The run graph: a device-side WHILE loop over fused steps, with the chunk-regeneration branch.
  * Writes the conditional handles into s (they are kernel arguments of the graph's nodes). */
-cudaError_t build_run_graph(DevSys& s, const LineGeom& g, cudaGraphExec_t* exec);
+cudaError_t build_run_graph(DevSys& s, const LineGeom& g, cudaGraphExec_t* exec, bool plain = false);
+/* Whether the system has the step kernels specialised for runs without activity, residual or
+ * recording (timeSteps / flowSteps of athermal Line1d / Particles systems). */
+bool plain_runs_apply(const DevSys& s);
 
 /* Small Line1d / Particles systems: a whole run in one launch of one thread-block cluster. */
 static const int SMALL_MAX_CTAS = 16;   /* cluster size limit (above 8 needs the non-portable opt-in) */
@@ -67,7 +70,7 @@ cudaError_t launch_thermal_draw(const DevSys& s, int from_ctl, int64_t inc, cuda
 int64_t thermal_tiles(int64_t N);
 
 /* One loop iteration launched kernel by kernel by the host (s.in_graph must be 0). */
-cudaError_t launch_iteration(const DevSys& s, const LineGeom& g, cudaStream_t st);
+cudaError_t launch_iteration(const DevSys& s, const LineGeom& g, cudaStream_t st, bool plain = false);
 
 /* NVTX range over one C-ABI call: each stepping / construction call shows as a named range on a
  * profiler timeline (header-only NVTX 3; a no-op unless a tool is attached). */

@@ -461,7 +461,7 @@ __device__ __forceinline__ void step_epilogue(const DevSys& s, StepShared& sh, i
  * from the old state.  State arrays are padded to a multiple of 1024 entries.  redo = 1: only CTAs
  * marked pending run (after k_regen moved their particles' windows).
  */
-template <int POT, int INTER, int PPT, unsigned SOFT = STEP_SOFT, bool TH = false>
+template <int POT, int INTER, int PPT, unsigned SOFT = STEP_SOFT, bool TH = false, bool PLAIN = false>
 __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_line(DevSys s, int redo)
 {
     __shared__ StepShared sh;
@@ -479,10 +479,12 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_line(DevSys s
         }
     }
     const int cur = sh.cur;
-    const bool act = (sh.flags & (RF_ACT | RF_TRUNCATE | RF_EVENT)) != 0;
-    const bool resid = (sh.flags & RF_RESID) != 0;
-    const bool ffsum = (sh.flags & RF_FFSUM) != 0;
-    const bool record = (sh.flags & RF_RECORD) != 0;
+    /* PLAIN: the instantiation for runs without activity, residual, frame-force sums or recording
+     * (timeSteps / flowSteps): that code compiled out */
+    const bool act = !PLAIN && (sh.flags & (RF_ACT | RF_TRUNCATE | RF_EVENT)) != 0;
+    const bool resid = !PLAIN && (sh.flags & RF_RESID) != 0;
+    const bool ffsum = !PLAIN && (sh.flags & RF_FFSUM) != 0;
+    const bool record = !PLAIN && (sh.flags & RF_RECORD) != 0;
     const int64_t rec_step = record ? ((volatile Ctl*)s.ctl)->step : 0;
     const double uf = sh.uf;
     const int64_t N = s.N;
@@ -731,6 +733,121 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_grid(DevSys s
         return;
     }
     step_epilogue(s, sh, EPI_GRID_STEP, 0.0, 0.0);
+}
+
+/*
+ * Line2d Laplace2d step with two rows per thread: CTA tile of 16 rows x 32 columns (blockDim 32 x 8,
+ * thread (x, y) owns rows 2y and 2y + 1 of column x).  The vertical neighbour between a thread's two
+ * particles comes from its own registers' shared-memory copy, and the recomputed halo is 96 positions
+ * per 512 particles instead of 80 per 256 for 8 x 32 tiles of one particle per thread.  Per particle
+ * the same operations in the same order as k_step_grid, so the same results.
+ */
+template <int POT, unsigned SOFT = STEP_SOFT>
+__global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_grid2(DevSys s, int redo)
+{
+    __shared__ StepShared sh;
+    __shared__ double sh_un[16][32];
+    if (!step_prologue(s, sh, true)) {
+        return;
+    }
+    const int64_t bid = blockIdx.x + (int64_t)blockIdx.y * gridDim.x;
+    if (redo) {
+        if (!s.cta_pending[bid]) {
+            return;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0 && threadIdx.y == 0) {
+            s.cta_pending[bid] = 0;
+        }
+    }
+    const int cur = sh.cur;
+    const bool act = (sh.flags & (RF_ACT | RF_TRUNCATE | RF_EVENT)) != 0;
+    const bool resid = (sh.flags & RF_RESID) != 0;
+    const double uf = sh.uf;
+    const int64_t R = s.rows, C = s.cols;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int64_t jc = (int64_t)blockIdx.x * 32 + tx;
+    const int64_t i0 = (int64_t)blockIdx.y * 16 + 2 * ty;
+    const double* u0 = s.u[cur];
+    const double* v0 = s.v[cur];
+    const double* a0 = s.a[cur];
+    double up[2], vr[2], ar[2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const int64_t i = i0 + q;
+        up[q] = vr[q] = ar[q] = 0.0;
+        if (i < R && jc < C) {
+            const int64_t p = i * C + jc;
+            vr[q] = v0[p];
+            ar[q] = a0[p];
+            up[q] = S_ADD(3, S_ADD(2, u0[p], S_MUL(0, s.dt, vr[q])), S_MUL(1, s.hdt2, ar[q]));
+            sh_un[2 * ty + q][tx] = up[q];
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const int64_t i = i0 + q;
+        if (!(i < R && jc < C)) {
+            continue;
+        }
+        const int64_t p = i * C + jc;
+        const int r = 2 * ty + q;
+        bool regen;
+        double4_32a w = well_of(s, p, up[q], act, sh, regen);
+        if (regen) {
+            if (!redo) {
+                sh.pending = 1;
+                int k = atomicAdd(&s.ctl->n_regen, 1);
+                s.regen_list[k] = (int32_t)p;
+            }
+            else {
+                atomicOr(&s.ctl->walk_flag, 1);
+            }
+        }
+        double ff;
+        double sfp = frame_pot<POT, SOFT>(s, w, up[q], uf, ff);
+        double uU = r > 0 ? sh_un[r - 1][tx] : u_next(s, u0, v0, a0, ((i + R - 1) % R) * C + jc);
+        double uD = (r < 15 && i + 1 < R) ? sh_un[r + 1][tx] : u_next(s, u0, v0, a0, ((i + 1) % R) * C + jc);
+        double uL = tx > 0 ? sh_un[r][tx - 1] : u_next(s, u0, v0, a0, i * C + (jc + C - 1) % C);
+        double uR = (tx < 31 && jc + 1 < C) ? sh_un[r][tx + 1] : u_next(s, u0, v0, a0, i * C + (jc + 1) % C);
+        double fi = scale(FQ_SUB(FQ_ADD(FQ_ADD(FQ_ADD(uU, uD), uL), uR), scale_pow2(up[q], 2, 4.0)), s.s_k);
+        double sfi = S_ADD(9, sfp, fi);
+        double vv, aa, f;
+        verlet_velocity<SOFT>(s, sfi, vr[q], ar[q], vv, aa, f);
+        s.u[cur ^ 1][p] = up[q];
+        s.v[cur ^ 1][p] = vv;
+        s.a[cur ^ 1][p] = aa;
+        if (is_nan_bits(up[q])) {
+            sh.nan = 1;
+        }
+        if (resid) {
+            s.sq2[p] = make_double2(mul_nospec(f, f), mul_nospec(ff, ff));
+        }
+    }
+    if (redo) {
+        /* the reduction kernel after the branch finalises; only the counters are committed here */
+        __syncthreads();
+        if (threadIdx.x == 0 && threadIdx.y == 0) {
+            if (sh.ds) {
+                atomicAdd((unsigned long long*)&s.ctl->s_sum, sh.ds);
+            }
+            if (sh.da) {
+                atomicAdd((unsigned long long*)&s.ctl->a_count, sh.da);
+            }
+            if (sh.nan) {
+                atomicOr(&s.ctl->nan_flag, 1);
+            }
+        }
+        return;
+    }
+    step_epilogue(s, sh, EPI_GRID_STEP, 0.0, 0.0);
+}
+
+/* Rows of a CTA tile of the 2d step kernel: 16 for Laplace2d (k_step_grid2), 8 otherwise. */
+static int64_t grid_tile_rows(const DevSys& s)
+{
+    return s.inter == INTER_LAPLACE2D ? 16 : 8;
 }
 
 /* Pairwise reduction of the 2d step's sq2 in flat-index order (1024 per CTA) + step finalisation. */
@@ -1343,7 +1460,7 @@ __global__ void __launch_bounds__(SMALL_THREADS_MAX + 32, 1) k_run_small(DevSys 
     __shared__ int sh_nan, sh_walk;
     __shared__ unsigned long long sh_ds, sh_da;
     /* window moves of this step shared by the CTA's particle threads (fwd_move_*) */
-    constexpr int SMALL_MOVES = 32;
+    constexpr int SMALL_MOVES = 64;
     __shared__ FwdMove sh_moves[SMALL_MOVES];
     __shared__ int sh_nmove;
 
@@ -1564,10 +1681,9 @@ __global__ void __launch_bounds__(SMALL_THREADS_MAX + 32, 1) k_run_small(DevSys 
                 }
             }
         }
-        /* window moves, in rounds of up to SMALL_MOVES: planned by their owners, drawn by all particle
-         * threads of the CTA, summed by their owners; moves that are not forward moves go through
-         * dev_align */
-        while (particle_bar_or(pt, any_mv ? 1 : 0)) {
+        if (particle_bar_or(pt, any_mv ? 1 : 0)) {
+            /* moves planned here are drawn by all particle threads of the CTA, then summed by their
+             * owners; the others (more than SMALL_MOVES, or not a forward move) go through dev_align */
             int slot[PPT];
 #pragma unroll
             for (int j = 0; j < PPT; ++j) {
@@ -1576,9 +1692,9 @@ __global__ void __launch_bounds__(SMALL_THREADS_MAX + 32, 1) k_run_small(DevSys 
                     int k = atomicAdd(&sh_nmove, 1);
                     if (k < SMALL_MOVES) {
                         FwdMove m;
-                        slot[j] = k;
                         if (fwd_move_plan(s, p0 + j, un[j], m)) {
                             sh_moves[k] = m;
+                            slot[j] = k;
                         }
                         else {
                             sh_moves[k].p = -1;
@@ -1594,18 +1710,13 @@ __global__ void __launch_bounds__(SMALL_THREADS_MAX + 32, 1) k_run_small(DevSys 
                 }
             }
             particle_bar(pt);
-            any_mv = false;
 #pragma unroll
             for (int j = 0; j < PPT; ++j) {
                 if (!mv[j]) {
                     continue;
                 }
-                if (slot[j] < 0) {
-                    any_mv = true; /* a later round */
-                    continue;
-                }
                 int64_t p = p0 + j;
-                if (sh_moves[slot[j]].p >= 0) {
+                if (slot[j] >= 0) {
                     fwd_move_sum(s, sh_moves[slot[j]]);
                 }
                 else {
@@ -1614,13 +1725,8 @@ __global__ void __launch_bounds__(SMALL_THREADS_MAX + 32, 1) k_run_small(DevSys 
                         sh_walk = 1;
                     }
                 }
-                mv[j] = false;
                 w[j] = s.wc[p];
                 count_move(p, gold[j], s.gidx[p]);
-            }
-            particle_bar(pt);
-            if (tid == 0) {
-                sh_nmove = 0;
             }
         }
 #pragma unroll
@@ -1832,21 +1938,41 @@ int64_t grid_reduce_ctas(int64_t N)
 int64_t step_ctas(const DevSys& s, const LineGeom& g)
 {
     if (inter_grid(s.inter)) {
-        return ((s.cols + 31) / 32) * ((s.rows + 7) / 8);
+        return ((s.cols + 31) / 32) * ((s.rows + grid_tile_rows(s) - 1) / grid_tile_rows(s));
     }
     return g.grid;
 }
 
 /* ------------------------------------------------------------- run graph */
 
-template <int POT, int INTER, bool TH = false>
+template <int POT, int INTER, bool TH = false, bool PLAIN = false>
 static void* line_kernel_t(int ppt)
 {
-    return ppt == 2 ? (void*)k_step_line<POT, INTER, 2, STEP_SOFT, TH> : (void*)k_step_line<POT, INTER, 1, STEP_SOFT, TH>;
+    return ppt == 2 ? (void*)k_step_line<POT, INTER, 2, STEP_SOFT, TH, PLAIN>
+                    : (void*)k_step_line<POT, INTER, 1, STEP_SOFT, TH, PLAIN>;
 }
 
-static void* step_kernel(const DevSys& s, const LineGeom& g)
+bool plain_runs_apply(const DevSys& s)
 {
+    return !s.f_th && (s.inter == INTER_LAPLACE1D || s.inter == INTER_NONE);
+}
+
+static void* step_kernel(const DevSys& s, const LineGeom& g, bool plain = false)
+{
+    if (plain && plain_runs_apply(s)) {
+        if (s.inter == INTER_LAPLACE1D) {
+            switch (s.pot) {
+                case POT_CUSPY: return line_kernel_t<POT_CUSPY, INTER_LAPLACE1D, false, true>(g.ppt);
+                case POT_SEMISMOOTH: return line_kernel_t<POT_SEMISMOOTH, INTER_LAPLACE1D, false, true>(g.ppt);
+                default: return line_kernel_t<POT_SMOOTH, INTER_LAPLACE1D, false, true>(g.ppt);
+            }
+        }
+        switch (s.pot) {
+            case POT_CUSPY: return line_kernel_t<POT_CUSPY, INTER_NONE, false, true>(g.ppt);
+            case POT_SEMISMOOTH: return line_kernel_t<POT_SEMISMOOTH, INTER_NONE, false, true>(g.ppt);
+            default: return line_kernel_t<POT_SMOOTH, INTER_NONE, false, true>(g.ppt);
+        }
+    }
     if (s.f_th) {
         /* RandomNormalForcing systems: Cuspy with Laplace1d, Quartic1d or no interactions */
         switch (s.inter) {
@@ -1869,9 +1995,9 @@ static void* step_kernel(const DevSys& s, const LineGeom& g)
     }
     if (s.inter == INTER_LAPLACE2D) {
         switch (s.pot) {
-            case POT_CUSPY: return (void*)k_step_grid<POT_CUSPY>;
-            case POT_SEMISMOOTH: return (void*)k_step_grid<POT_SEMISMOOTH>;
-            default: return (void*)k_step_grid<POT_SMOOTH>;
+            case POT_CUSPY: return (void*)k_step_grid2<POT_CUSPY>;
+            case POT_SEMISMOOTH: return (void*)k_step_grid2<POT_SEMISMOOTH>;
+            default: return (void*)k_step_grid2<POT_SMOOTH>;
         }
     }
     if (s.inter == INTER_LAPLACE1D) {
@@ -1921,19 +2047,19 @@ static cudaError_t add_conditional(cudaGraphNode_t* node, cudaGraph_t graph, con
  * profile kernels inside conditional graphs): pass 1, the regeneration kernel and the redo are always
  * launched; the latter two do nothing when no CTA is pending.
  */
-cudaError_t launch_iteration(const DevSys& s, const LineGeom& g0, cudaStream_t st)
+cudaError_t launch_iteration(const DevSys& s, const LineGeom& g0, cudaStream_t st, bool plain)
 {
     bool is2d = inter_grid(s.inter);
     dim3 grid, block;
     if (is2d) {
-        grid = dim3((unsigned)((s.cols + 31) / 32), (unsigned)((s.rows + 7) / 8));
+        grid = dim3((unsigned)((s.cols + 31) / 32), (unsigned)((s.rows + grid_tile_rows(s) - 1) / grid_tile_rows(s)));
         block = dim3(32, 8);
     }
     else {
         grid = dim3((unsigned)g0.grid);
         block = dim3((unsigned)g0.threads);
     }
-    void* fstep = step_kernel(s, g0);
+    void* fstep = step_kernel(s, g0, plain);
     int pass1 = 0, pass2 = 1;
     void* args1[] = {(void*)&s, (void*)&pass1};
     void* args2[] = {(void*)&s, (void*)&pass2};
@@ -1973,7 +2099,7 @@ cudaError_t launch_iteration(const DevSys& s, const LineGeom& g0, cudaStream_t s
  * The run graph: WHILE(h_while) { step pass 1 ; IF(h_if) { regenerate windows ; redo pending CTAs } ;
  * [2d: reduce + finalise] }.  `s` is updated with the two conditional handles (kernel arguments).
  */
-cudaError_t build_run_graph(DevSys& s, const LineGeom& g0, cudaGraphExec_t* exec)
+cudaError_t build_run_graph(DevSys& s, const LineGeom& g0, cudaGraphExec_t* exec, bool plain)
 {
     cudaGraph_t g;
     cudaError_t e = cudaGraphCreate(&g, 0);
@@ -1993,14 +2119,14 @@ cudaError_t build_run_graph(DevSys& s, const LineGeom& g0, cudaGraphExec_t* exec
     bool is2d = inter_grid(s.inter);
     dim3 grid, block;
     if (is2d) {
-        grid = dim3((unsigned)((s.cols + 31) / 32), (unsigned)((s.rows + 7) / 8));
+        grid = dim3((unsigned)((s.cols + 31) / 32), (unsigned)((s.rows + grid_tile_rows(s) - 1) / grid_tile_rows(s)));
         block = dim3(32, 8);
     }
     else {
         grid = dim3((unsigned)g0.grid);
         block = dim3((unsigned)g0.threads);
     }
-    void* fstep = step_kernel(s, g0);
+    void* fstep = step_kernel(s, g0, plain);
     int pass1 = 0, pass2 = 1;
     void* args1[] = {(void*)&s, (void*)&pass1};
     void* args2[] = {(void*)&s, (void*)&pass2};
