@@ -54,6 +54,7 @@ struct fqsb_system {
     int64_t ring_cap;
     cudaGraphExec_t graph;
     cudaGraphExec_t graph_plain; /* the run graph of runs without activity, residual or recording */
+    cudaGraphExec_t graph_resid; /* the run graph of runs with the residual only (minimise) */
     cudaGraphExec_t graph_np; /* the no-passing minimiser's run graph */
     int graph_k;
     bool use_graph; /* false when FQSB_NO_GRAPH=1: host-driven launches (profiling) */
@@ -540,17 +541,18 @@ static int materialise_forces(fqsb_system* h)
 static const uint64_t RUN_BUDGET_NS = 200ull * 1000ull * 1000ull;
 static const int64_t RING_MIN = 1024;
 
-static int ensure_graph(fqsb_system* h, bool plain = false)
+static int ensure_graph(fqsb_system* h, int mode = KMODE_GENERAL)
 {
     if (!h->use_graph) {
         h->d.in_graph = 0;
         return FQSB_OK;
     }
-    if (plain) {
-        if (!h->graph_plain) {
+    if (mode != KMODE_GENERAL) {
+        cudaGraphExec_t* g = mode == KMODE_PLAIN ? &h->graph_plain : &h->graph_resid;
+        if (!*g) {
             /* built from a copy: its conditional handles are its own kernels' arguments */
             DevSys d = h->d;
-            CU(h, build_run_graph(d, h->lg, &h->graph_plain, true));
+            CU(h, build_run_graph(d, h->lg, g, mode));
         }
         return FQSB_OK;
     }
@@ -609,6 +611,10 @@ static int run(fqsb_system* h, int64_t max_steps, int flags, double tol, int64_t
             cudaGraphExecDestroy(h->graph_plain);
             h->graph_plain = nullptr;
         }
+        if (h->graph_resid) {
+            cudaGraphExecDestroy(h->graph_resid);
+            h->graph_resid = nullptr;
+        }
         if (h->graph_np) {
             cudaGraphExecDestroy(h->graph_np);
             h->graph_np = nullptr;
@@ -616,9 +622,11 @@ static int run(fqsb_system* h, int64_t max_steps, int flags, double tol, int64_t
     }
     bool use_small = np == nullptr && h->small_ok && io == nullptr && !(flags & (RF_SCHEDULE | RF_RECORD | RF_FFSUM)) &&
                      !((flags & RF_RESID) && niter_tol > SMALL_RING_MAX);
-    /* runs without activity, residual, frame-force sums or recording take the specialised step kernels */
-    const bool plain = np == nullptr && plain_runs_apply(h->d) &&
-                       !(flags & (RF_RESID | RF_FFSUM | RF_ACT | RF_TRUNCATE | RF_EVENT | RF_RECORD));
+    /* runs without activity, frame-force sums or recording take the specialised step kernels */
+    int kmode = KMODE_GENERAL;
+    if (np == nullptr && plain_runs_apply(h->d) && !(flags & (RF_FFSUM | RF_ACT | RF_TRUNCATE | RF_EVENT | RF_RECORD))) {
+        kmode = (flags & RF_RESID) ? KMODE_RESID : KMODE_PLAIN;
+    }
     if (np) {
         if (h->use_graph && !h->graph_np) {
             CU(h, build_nopass_graph(h->d, h->lg, *np, &h->graph_np));
@@ -628,7 +636,7 @@ static int run(fqsb_system* h, int64_t max_steps, int flags, double tol, int64_t
         }
     }
     else if (!use_small) {
-        rc = ensure_graph(h, plain);
+        rc = ensure_graph(h, kmode);
         if (rc) {
             return rc;
         }
@@ -701,7 +709,7 @@ static int run(fqsb_system* h, int64_t max_steps, int flags, double tol, int64_t
                 cudaGetLastError();
                 h->small_ok = false;
                 use_small = false;
-                rc = ensure_graph(h, plain);
+                rc = ensure_graph(h, kmode);
                 if (rc) {
                     return rc;
                 }
@@ -710,11 +718,14 @@ static int run(fqsb_system* h, int64_t max_steps, int flags, double tol, int64_t
             CU(h, le);
         }
         else if (h->use_graph) {
-            CU(h, cudaGraphLaunch(plain ? h->graph_plain : h->graph, h->stream));
+            CU(h, cudaGraphLaunch(kmode == KMODE_PLAIN ? h->graph_plain
+                                  : kmode == KMODE_RESID ? h->graph_resid
+                                                         : h->graph,
+                                  h->stream));
         }
         else {
             for (int i = 0; i < 64; ++i) {
-                CU(h, launch_iteration(h->d, h->lg, h->stream, plain));
+                CU(h, launch_iteration(h->d, h->lg, h->stream, kmode));
             }
         }
         first_launch = false;
@@ -796,6 +807,9 @@ static void free_all(fqsb_system* h)
     if (h->graph_plain) {
         cudaGraphExecDestroy(h->graph_plain);
     }
+    if (h->graph_resid) {
+        cudaGraphExecDestroy(h->graph_resid);
+    }
     if (h->graph_np) {
         cudaGraphExecDestroy(h->graph_np);
     }
@@ -860,6 +874,7 @@ extern "C" int fqsb_create(const fqsb_config* cfg, fqsb_system** out)
     h->ring_cap = 0;
     h->graph = nullptr;
     h->graph_plain = nullptr;
+    h->graph_resid = nullptr;
     h->graph_np = nullptr;
     h->graph_k = 0;
     {
@@ -1536,6 +1551,10 @@ extern "C" int fqsb_set_random_forcing(fqsb_system* h, double mean, double stdde
         cudaGraphExecDestroy(h->graph_plain);
         h->graph_plain = nullptr;
     }
+    if (h->graph_resid) {
+        cudaGraphExecDestroy(h->graph_resid);
+        h->graph_resid = nullptr;
+    }
     h->small_ok = false;
     int rc = updated_inc(h); /* the constructor's refresh */
     return rc ? rc : sync(h);
@@ -1945,6 +1964,10 @@ extern "C" int fqsb_set_parameters(fqsb_system* h, double mu, double k_interacti
     if (h->graph_plain) {
         cudaGraphExecDestroy(h->graph_plain);
         h->graph_plain = nullptr;
+    }
+    if (h->graph_resid) {
+        cudaGraphExecDestroy(h->graph_resid);
+        h->graph_resid = nullptr;
     }
     h->stored = false;
     return sync(h);

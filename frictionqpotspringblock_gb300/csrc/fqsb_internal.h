@@ -34,9 +34,12 @@ int64_t step_ctas(const DevSys& s, const LineGeom& g);
 
 /* The run graph: a device-side WHILE loop over fused steps, with the chunk-regeneration branch.
  * Writes the conditional handles into s (they are kernel arguments of the graph's nodes). */
-cudaError_t build_run_graph(DevSys& s, const LineGeom& g, cudaGraphExec_t* exec, bool plain = false);
-/* Whether the system has the step kernels specialised for runs without activity, residual or
- * recording (timeSteps / flowSteps of athermal Line1d / Particles systems). */
+/* Step-kernel instantiations: the general one, and for athermal Line1d / Particles systems two
+ * specialised ones -- runs without activity, residual, frame-force sums or recording (timeSteps /
+ * flowSteps), and runs with the residual only (minimise) -- with the other code compiled out. */
+enum : int { KMODE_GENERAL = 0, KMODE_PLAIN = 1, KMODE_RESID = 2 };
+cudaError_t build_run_graph(DevSys& s, const LineGeom& g, cudaGraphExec_t* exec, int mode = KMODE_GENERAL);
+/* Whether the system has the specialised step kernels (athermal Line1d / Particles systems). */
 bool plain_runs_apply(const DevSys& s);
 
 /* Small Line1d / Particles systems: a whole run in one launch of one thread-block cluster. */
@@ -70,7 +73,7 @@ cudaError_t launch_thermal_draw(const DevSys& s, int from_ctl, int64_t inc, cuda
 int64_t thermal_tiles(int64_t N);
 
 /* One loop iteration launched kernel by kernel by the host (s.in_graph must be 0). */
-cudaError_t launch_iteration(const DevSys& s, const LineGeom& g, cudaStream_t st, bool plain = false);
+cudaError_t launch_iteration(const DevSys& s, const LineGeom& g, cudaStream_t st, int mode = KMODE_GENERAL);
 
 /* NVTX range over one C-ABI call: each stepping / construction call shows as a named range on a
  * profiler timeline (header-only NVTX 3; a no-op unless a tool is attached). */

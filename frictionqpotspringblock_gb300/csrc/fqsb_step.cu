@@ -461,7 +461,7 @@ __device__ __forceinline__ void step_epilogue(const DevSys& s, StepShared& sh, i
  * from the old state.  State arrays are padded to a multiple of 1024 entries.  redo = 1: only CTAs
  * marked pending run (after k_regen moved their particles' windows).
  */
-template <int POT, int INTER, int PPT, unsigned SOFT = STEP_SOFT, bool TH = false, bool PLAIN = false>
+template <int POT, int INTER, int PPT, unsigned SOFT = STEP_SOFT, bool TH = false, int MODE = KMODE_GENERAL>
 __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_line(DevSys s, int redo)
 {
     __shared__ StepShared sh;
@@ -479,12 +479,13 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_line(DevSys s
         }
     }
     const int cur = sh.cur;
-    /* PLAIN: the instantiation for runs without activity, residual, frame-force sums or recording
-     * (timeSteps / flowSteps): that code compiled out */
-    const bool act = !PLAIN && (sh.flags & (RF_ACT | RF_TRUNCATE | RF_EVENT)) != 0;
-    const bool resid = !PLAIN && (sh.flags & RF_RESID) != 0;
-    const bool ffsum = !PLAIN && (sh.flags & RF_FFSUM) != 0;
-    const bool record = !PLAIN && (sh.flags & RF_RECORD) != 0;
+    /* KMODE_PLAIN: the instantiation for runs without activity, residual, frame-force sums or recording
+     * (timeSteps / flowSteps); KMODE_RESID: with the residual only (minimise); the rest compiled out */
+    const bool general = MODE == KMODE_GENERAL;
+    const bool act = general && (sh.flags & (RF_ACT | RF_TRUNCATE | RF_EVENT)) != 0;
+    const bool resid = MODE == KMODE_RESID || (general && (sh.flags & RF_RESID) != 0);
+    const bool ffsum = general && (sh.flags & RF_FFSUM) != 0;
+    const bool record = general && (sh.flags & RF_RECORD) != 0;
     const int64_t rec_step = record ? ((volatile Ctl*)s.ctl)->step : 0;
     const double uf = sh.uf;
     const int64_t N = s.N;
@@ -1945,11 +1946,28 @@ int64_t step_ctas(const DevSys& s, const LineGeom& g)
 
 /* ------------------------------------------------------------- run graph */
 
-template <int POT, int INTER, bool TH = false, bool PLAIN = false>
+template <int POT, int INTER, bool TH = false, int MODE = KMODE_GENERAL>
 static void* line_kernel_t(int ppt)
 {
-    return ppt == 2 ? (void*)k_step_line<POT, INTER, 2, STEP_SOFT, TH, PLAIN>
-                    : (void*)k_step_line<POT, INTER, 1, STEP_SOFT, TH, PLAIN>;
+    return ppt == 2 ? (void*)k_step_line<POT, INTER, 2, STEP_SOFT, TH, MODE>
+                    : (void*)k_step_line<POT, INTER, 1, STEP_SOFT, TH, MODE>;
+}
+
+template <int MODE>
+static void* special_kernel(const DevSys& s, const LineGeom& g)
+{
+    if (s.inter == INTER_LAPLACE1D) {
+        switch (s.pot) {
+            case POT_CUSPY: return line_kernel_t<POT_CUSPY, INTER_LAPLACE1D, false, MODE>(g.ppt);
+            case POT_SEMISMOOTH: return line_kernel_t<POT_SEMISMOOTH, INTER_LAPLACE1D, false, MODE>(g.ppt);
+            default: return line_kernel_t<POT_SMOOTH, INTER_LAPLACE1D, false, MODE>(g.ppt);
+        }
+    }
+    switch (s.pot) {
+        case POT_CUSPY: return line_kernel_t<POT_CUSPY, INTER_NONE, false, MODE>(g.ppt);
+        case POT_SEMISMOOTH: return line_kernel_t<POT_SEMISMOOTH, INTER_NONE, false, MODE>(g.ppt);
+        default: return line_kernel_t<POT_SMOOTH, INTER_NONE, false, MODE>(g.ppt);
+    }
 }
 
 bool plain_runs_apply(const DevSys& s)
@@ -1957,21 +1975,10 @@ bool plain_runs_apply(const DevSys& s)
     return !s.f_th && (s.inter == INTER_LAPLACE1D || s.inter == INTER_NONE);
 }
 
-static void* step_kernel(const DevSys& s, const LineGeom& g, bool plain = false)
+static void* step_kernel(const DevSys& s, const LineGeom& g, int mode = KMODE_GENERAL)
 {
-    if (plain && plain_runs_apply(s)) {
-        if (s.inter == INTER_LAPLACE1D) {
-            switch (s.pot) {
-                case POT_CUSPY: return line_kernel_t<POT_CUSPY, INTER_LAPLACE1D, false, true>(g.ppt);
-                case POT_SEMISMOOTH: return line_kernel_t<POT_SEMISMOOTH, INTER_LAPLACE1D, false, true>(g.ppt);
-                default: return line_kernel_t<POT_SMOOTH, INTER_LAPLACE1D, false, true>(g.ppt);
-            }
-        }
-        switch (s.pot) {
-            case POT_CUSPY: return line_kernel_t<POT_CUSPY, INTER_NONE, false, true>(g.ppt);
-            case POT_SEMISMOOTH: return line_kernel_t<POT_SEMISMOOTH, INTER_NONE, false, true>(g.ppt);
-            default: return line_kernel_t<POT_SMOOTH, INTER_NONE, false, true>(g.ppt);
-        }
+    if (mode != KMODE_GENERAL && plain_runs_apply(s)) {
+        return mode == KMODE_PLAIN ? special_kernel<KMODE_PLAIN>(s, g) : special_kernel<KMODE_RESID>(s, g);
     }
     if (s.f_th) {
         /* RandomNormalForcing systems: Cuspy with Laplace1d, Quartic1d or no interactions */
@@ -2047,7 +2054,7 @@ static cudaError_t add_conditional(cudaGraphNode_t* node, cudaGraph_t graph, con
  * profile kernels inside conditional graphs): pass 1, the regeneration kernel and the redo are always
  * launched; the latter two do nothing when no CTA is pending.
  */
-cudaError_t launch_iteration(const DevSys& s, const LineGeom& g0, cudaStream_t st, bool plain)
+cudaError_t launch_iteration(const DevSys& s, const LineGeom& g0, cudaStream_t st, int mode)
 {
     bool is2d = inter_grid(s.inter);
     dim3 grid, block;
@@ -2059,7 +2066,7 @@ cudaError_t launch_iteration(const DevSys& s, const LineGeom& g0, cudaStream_t s
         grid = dim3((unsigned)g0.grid);
         block = dim3((unsigned)g0.threads);
     }
-    void* fstep = step_kernel(s, g0, plain);
+    void* fstep = step_kernel(s, g0, mode);
     int pass1 = 0, pass2 = 1;
     void* args1[] = {(void*)&s, (void*)&pass1};
     void* args2[] = {(void*)&s, (void*)&pass2};
@@ -2099,7 +2106,7 @@ cudaError_t launch_iteration(const DevSys& s, const LineGeom& g0, cudaStream_t s
  * The run graph: WHILE(h_while) { step pass 1 ; IF(h_if) { regenerate windows ; redo pending CTAs } ;
  * [2d: reduce + finalise] }.  `s` is updated with the two conditional handles (kernel arguments).
  */
-cudaError_t build_run_graph(DevSys& s, const LineGeom& g0, cudaGraphExec_t* exec, bool plain)
+cudaError_t build_run_graph(DevSys& s, const LineGeom& g0, cudaGraphExec_t* exec, int mode)
 {
     cudaGraph_t g;
     cudaError_t e = cudaGraphCreate(&g, 0);
@@ -2126,7 +2133,7 @@ cudaError_t build_run_graph(DevSys& s, const LineGeom& g0, cudaGraphExec_t* exec
         grid = dim3((unsigned)g0.grid);
         block = dim3((unsigned)g0.threads);
     }
-    void* fstep = step_kernel(s, g0, plain);
+    void* fstep = step_kernel(s, g0, mode);
     int pass1 = 0, pass2 = 1;
     void* args1[] = {(void*)&s, (void*)&pass1};
     void* args2[] = {(void*)&s, (void*)&pass2};
