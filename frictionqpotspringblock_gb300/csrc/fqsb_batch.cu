@@ -115,8 +115,10 @@ __device__ double2 inst_tree(const double2* partials, int64_t G, double* sh)
     }
     else {
         int64_t per = P / T, lo = (int64_t)threadIdx.x * per;
-        x = serial_tree([&](int64_t i) { return i < G ? __ldcg(partials + i).x : 0.0; }, lo, per);
-        y = serial_tree([&](int64_t i) { return i < G ? __ldcg(partials + i).y : 0.0; }, lo, per);
+        const double2 t = serial_tree2(
+            [&](int64_t i) { return i < G ? __ldcg(partials + i) : make_double2(0.0, 0.0); }, lo, per);
+        x = t.x;
+        y = t.y;
     }
     double sx = cta_tree(x, sh);
     __syncthreads();

@@ -14,6 +14,7 @@
  * f_damping and f) until the next operation that calls updated_u.
  */
 #include <algorithm>
+#include <cstdint>
 #include <cstdlib>
 #include <cmath>
 #include <cstdio>
@@ -60,6 +61,7 @@ struct fqsb_system {
     bool use_graph; /* false when FQSB_NO_GRAPH=1: host-driven launches (profiling) */
     SmallGeom sg;   /* one-cluster run kernel of small systems */
     bool small_ok;  /* N fits one cluster, 1d ring or no interactions, not disabled by FQSB_NO_SMALL=1 */
+    bool nx_dirty;  /* the next-window buffers may be out of date: refresh before the next small run */
     std::string err;
     /* adjoint tape */
     int64_t adj_T, adj_K, adj_last, adj_nseg;
@@ -114,6 +116,9 @@ __global__ void k_init_chunk(DevSys d)
         return;
     }
     d.anc_kind[p] = 0;
+    if (d.nx_end) {
+        d.nx_end[p] = INT64_MIN; /* no next-window buffer yet */
+    }
     double* y = d.data + p * d.W;
     double acc;
     seq_fill(d, p, 0, d.W, y, &acc);
@@ -369,6 +374,9 @@ __global__ void k_restore(DevSys d, const uint64_t* state, const double* value, 
         return;
     }
     d.anc_kind[p] = 1;
+    if (d.nx_end) {
+        d.nx_end[p] = INT64_MIN; /* another sequence: the next-window buffer is void */
+    }
     d.anc_k[p] = index[p];
     d.anc_state[p] = state[p];
     d.anc_val[p] = value[p];
@@ -703,6 +711,10 @@ static int run(fqsb_system* h, int64_t max_steps, int flags, double tol, int64_t
             }
         }
         else if (use_small) {
+            if (h->nx_dirty) {
+                CU(h, launch_next_window(h->d, h->stream));
+                h->nx_dirty = false;
+            }
             cudaError_t le = launch_small_run(h->d, h->sg, h->stream);
             if (first_launch && (le == cudaErrorInvalidClusterSize || le == cudaErrorLaunchOutOfResources)) {
                 /* the cluster could not be scheduled now (nothing ran): this handle uses the graph path */
@@ -733,6 +745,9 @@ static int run(fqsb_system* h, int64_t max_steps, int flags, double tol, int64_t
         rc = sync(h);
         if (rc) {
             return rc;
+        }
+        if (use_small && c->nx_stale) {
+            h->nx_dirty = true;
         }
         if (c->done || c->error) {
             break;
@@ -790,7 +805,7 @@ static void free_all(fqsb_system* h)
         return;
     }
     DevSys& d = h->d;
-    void* ptrs[] = {d.data, d.start, d.cidx, d.gidx, d.wc, d.acc_end, d.anc_kind, d.anc_k, d.anc_state, d.anc_val,
+    void* ptrs[] = {d.data, d.nx, d.nx_end, d.start, d.cidx, d.gidx, d.wc, d.acc_end, d.anc_kind, d.anc_k, d.anc_state, d.anc_val,
                     d.u[0], d.u[1], d.v[0], d.v[1], d.a[0], d.a[1], d.ctl, d.ring, d.partials, d.i_n, d.sq2,
                     d.cta_pending, d.regen_list, (void*)d.lr_pref, d.f_th, d.th_next, (void*)d.th_dinc, d.th_cnt,
                     d.th_list, d.th,
@@ -975,6 +990,11 @@ extern "C" int fqsb_create(const fqsb_config* cfg, fqsb_system** out)
     size_t nd = sizeof(double) * (size_t)N;
     size_t ndp = sizeof(double) * (size_t)padded(N);
     ALLOC(d.data, sizeof(double) * (size_t)N * (size_t)d.W);
+    if (h->small_ok && N * d.W <= NX_MAX_VALUES) {
+        ALLOC(d.nx, sizeof(double) * (size_t)N * (size_t)d.W);
+        ALLOC(d.nx_end, sizeof(int64_t) * (size_t)N);
+        h->nx_dirty = true;
+    }
     ALLOC(d.start, sizeof(int64_t) * (size_t)N);
     ALLOC(d.cidx, sizeof(int32_t) * (size_t)N);
     ALLOC(d.gidx, sizeof(int64_t) * (size_t)N);
@@ -1922,6 +1942,7 @@ extern "C" int fqsb_chunk_restore(fqsb_system* h, const uint64_t* state, const d
     CU(h, cudaMemcpyAsync(di, index, sizeof(int64_t) * (size_t)N, cudaMemcpyHostToDevice, h->stream));
     k_restore<<<blocks_for(N, 64), 64, 0, h->stream>>>(h->d, ds, dv, di);
     CU(h, cudaGetLastError());
+    h->nx_dirty = true;
     CU(h, cudaFreeAsync(buf, h->stream));
     return sync(h);
 }

@@ -99,7 +99,7 @@ struct Ctl {
     uint32_t ticket_redo;
     int32_t n_pending_cta; /* CTAs of this step with a particle whose chunk window must move */
     int32_t n_regen;       /* particles of this step whose chunk window must move */
-    int32_t pad2;
+    int32_t nx_stale;      /* the one-cluster kernel moved a window: next-window buffers to refresh */
     int64_t launch_steps;  /* steps done in the current graph launch */
     uint64_t launch_t0;    /* %globaltimer at the first step of the current graph launch */
     uint64_t budget_ns;    /* device time after which a graph launch yields back to the host */
@@ -192,6 +192,8 @@ struct DevSys {
     int64_t* gidx;
     double4_32a* wc;
     double* acc_end;
+    double* nx;      /* next-window buffer [N, W] of small systems (next_window_ready), or NULL */
+    int64_t* nx_end; /* window end the buffer of particle p follows */
     uint8_t* anc_kind;
     int64_t* anc_k;
     uint64_t* anc_state;
@@ -635,7 +637,29 @@ static __device__ __noinline__ bool dev_align(const DevSys& s, int64_t p, double
 struct FwdMove {
     int64_t p, ns, keep;
     uint64_t st_first; /* pcg32 state whose output is the draw of index old end + 1 */
+    int32_t next;      /* the new slots come from the next-window buffer (next_window_ready) */
+    int32_t pad;
 };
+
+/* Forward shift of a window's kept values, y[j] = y[j + sh] for j < keep, in blocks of 16 loads
+ * ahead of their stores (a later block reads only slots above the ones written so far). */
+static __device__ __noinline__ void window_shift(double* y, int64_t keep, int64_t sh)
+{
+    constexpr int B = 16;
+    for (int64_t j0 = 0; j0 < keep; j0 += B) {
+        double t[B];
+#pragma unroll
+        for (int i = 0; i < B; ++i) {
+            t[i] = j0 + i < keep ? y[j0 + i + sh] : 0.0;
+        }
+#pragma unroll
+        for (int i = 0; i < B; ++i) {
+            if (j0 + i < keep) {
+                y[j0 + i] = t[i];
+            }
+        }
+    }
+}
 
 /* Plans the move of particle p to target u; on success also copies the kept values down. */
 __device__ __forceinline__ bool fwd_move_plan(const DevSys& s, int64_t p, double u, FwdMove& m)
@@ -673,40 +697,44 @@ __device__ __forceinline__ bool fwd_move_plan(const DevSys& s, int64_t p, double
     if (ns <= start || keep <= 0 || end < ko) {
         return false;
     }
-    for (int64_t j = 0; j < keep; ++j) {
-        y[j] = y[j + (ns - start)];
-    }
+    window_shift(y, keep, ns - start);
     m.p = p;
     m.ns = ns;
     m.keep = keep;
     m.st_first = pcg_advance(sto, (uint64_t)(end + 1 - ko));
+    m.next = 0;
     return true;
 }
 
-/* Draws of one planned move: thread `lane` of `nlanes` writes the draws of window slots
- * keep + lane, keep + lane + nlanes, ... (one jump-ahead, then strides of nlanes steps: the
- * stride map x -> a x + c with c = advance(0, nlanes), a = advance(1, nlanes) - c). */
-static __device__ __noinline__ void fwd_move_draws(const DevSys& s, const FwdMove& m, int lane, int nlanes,
-                                                   uint64_t sa, uint64_t sc)
+/* Draws of cnt consecutive sequence indices into dst[0..cnt), the first from pcg32 state st_first:
+ * thread `lane` of `nlanes` writes slots lane, lane + nlanes, ... (one jump-ahead, then strides of
+ * nlanes steps: the stride map x -> a x + c with c = advance(0, nlanes), a = advance(1, nlanes) - c). */
+static __device__ __noinline__ void seq_draws(const DevSys& s, double* dst, int64_t cnt, uint64_t st_first, int lane,
+                                              int nlanes, uint64_t sa, uint64_t sc)
 {
-    const int64_t W = s.W;
-    double* y = s.data + m.p * W;
     /* two draws per iteration (slots j and j + nlanes), inlined, so that their long dependency chains
      * overlap; stride 2 nlanes: x -> sa2 x + sc2 */
     const uint64_t sa2 = sa * sa, sc2 = sa * sc + sc;
-    uint64_t st0 = pcg_advance(m.st_first, (uint64_t)lane);
+    uint64_t st0 = pcg_advance(st_first, (uint64_t)lane);
     uint64_t st1 = sa * st0 + sc;
     const bool delta = s.dist == DIST_DELTA;
-    for (int64_t j = m.keep + lane; j < W; j += 2 * (int64_t)nlanes) {
+    for (int64_t j = lane; j < cnt; j += 2 * (int64_t)nlanes) {
         const double d0 = dev_transform_inl(s, delta ? 0u : pcg_output(st0));
         const double d1 = dev_transform_inl(s, delta ? 0u : pcg_output(st1));
-        y[j] = d0;
-        if (j + nlanes < W) {
-            y[j + nlanes] = d1;
+        dst[j] = d0;
+        if (j + nlanes < cnt) {
+            dst[j + nlanes] = d1;
         }
         st0 = sa2 * st0 + sc2;
         st1 = sa2 * st1 + sc2;
     }
+}
+
+/* Draws of one planned move: window slots keep .. W - 1 */
+__device__ __forceinline__ void fwd_move_draws(const DevSys& s, const FwdMove& m, int lane, int nlanes, uint64_t sa,
+                                               uint64_t sc)
+{
+    seq_draws(s, s.data + m.p * s.W + m.keep, s.W - m.keep, m.st_first, lane, nlanes, sa, sc);
 }
 
 /* The running sum of one planned move over its drawn slots, in the sequence's order (walker_next's
@@ -766,6 +794,88 @@ __device__ __forceinline__ void fwd_move_sum(const DevSys& s, const FwdMove& m)
     }
     s.start[p] = m.ns;
     s.acc_end[p] = acc;
+    const int64_t li = s.margin;
+    s.cidx[p] = (int32_t)li;
+    s.gidx[p] = m.ns + li;
+    s.wc[p] = make_wc(s, y[li], y[li + 1]);
+}
+
+/*
+ * Next-window buffer of the one-cluster kernel of small systems.  nx[p * W + j] holds y_k of the
+ * W sequence indices k = end + 1 + j after the window end `end` = nx_end[p], computed ahead of the
+ * run (k_next_window) by the rules of fwd_move_sum, so that a forward move inside the run copies its
+ * new slots instead of drawing them: a move then costs a copy, not W - keep distribution transforms
+ * on one SM while the whole cluster waits.  Held for indices past the initial region only (there the
+ * accumulator equals y_k, which fixes acc_end after the move); other windows keep the drawn moves.
+ */
+__device__ __forceinline__ bool next_window_ready(const DevSys& s, int64_t p)
+{
+    return s.nx != nullptr && s.nx_end[p] == s.start[p] + s.W - 1;
+}
+
+/* Whether the buffer can hold the indices after window end `end` of particle p; also the origin */
+__device__ __forceinline__ bool next_window_applies(const DevSys& s, int64_t p, int64_t end, int& kind, int64_t& ko,
+                                                    uint64_t& sto)
+{
+    seq_origin(s, p, kind, ko, sto);
+    return end >= ko && (kind != 0 || end + 1 >= s.n0);
+}
+
+/* The running sum over drawn slots nx[p * W ...] after window end `end`, in place (one thread) */
+static __device__ __noinline__ void next_window_sum(const DevSys& s, int64_t p, int64_t end, int kind)
+{
+    const int64_t W = s.W, n0 = s.n0;
+    double* y = s.nx + p * W;
+    const double o = off_of(s, p);
+    double acc = s.acc_end[p];
+    constexpr int B = 16;
+    for (int64_t j0 = 0; j0 < W; j0 += B) {
+        double d[B];
+#pragma unroll
+        for (int i = 0; i < B; ++i) {
+            d[i] = j0 + i < W ? __ldcg(y + j0 + i) : 0.0;
+        }
+#pragma unroll
+        for (int i = 0; i < B; ++i) {
+            if (j0 + i >= W) {
+                break;
+            }
+            if (kind == 0 && end + 1 + j0 + i == n0) {
+                acc = FQ_ADD(FQ_ADD(acc, o), d[i]);
+            }
+            else {
+                acc = FQ_ADD(acc, d[i]);
+            }
+            d[i] = acc;
+        }
+#pragma unroll
+        for (int i = 0; i < B; ++i) {
+            if (j0 + i < W) {
+                y[j0 + i] = d[i];
+            }
+        }
+    }
+}
+
+/* A planned move whose new slots are in the next-window buffer: thread `lane` of `nlanes` copies
+ * slots keep + lane, keep + lane + nlanes, ... */
+__device__ __forceinline__ void fwd_move_copy(const DevSys& s, const FwdMove& m, int lane, int nlanes)
+{
+    const int64_t W = s.W;
+    double* y = s.data + m.p * W;
+    const double* x = s.nx + m.p * W;
+    for (int64_t j = m.keep + lane; j < W; j += nlanes) {
+        y[j] = __ldcg(x + (j - m.keep));
+    }
+}
+
+/* The window bookkeeping of a copied move, as fwd_move_sum leaves it */
+__device__ __forceinline__ void fwd_move_finish(const DevSys& s, const FwdMove& m)
+{
+    const int64_t W = s.W, p = m.p;
+    double* y = s.data + p * W;
+    s.start[p] = m.ns;
+    s.acc_end[p] = __ldcg(s.nx + p * W + (W - 1 - m.keep));
     const int64_t li = s.margin;
     s.cidx[p] = (int32_t)li;
     s.gidx[p] = m.ns + li;
@@ -1011,41 +1121,64 @@ __device__ __forceinline__ double cta_tree(double x, double* sh)
     return x;
 }
 
-/* Two cta_tree sums at once (one pair of barriers; the shuffles of x and y interleave).  Same trees,
- * same results as cta_tree(x) and cta_tree(y).  sh needs 2 * blockDim/32 doubles. */
+/*
+ * Two cta_tree sums at once, same trees and results as cta_tree(x) and cta_tree(y), with fewer fp64
+ * instructions: the fp64 pipe takes a warp instruction whatever its active lanes, so the x and y
+ * trees share instructions.  In a warp, the first level (16 x pairs and 16 y pairs) is one full-warp
+ * addition leaving [x partials | y partials] in lanes 0-15 | 16-31, and each further level
+ * v_l = v_2l + v_2l+1 pairs that concatenation in order (x in the lower, y in the upper half of the
+ * active lanes); the CTA level does the same over [warp x sums | warp y sums].  Result valid in
+ * thread 0.  sh needs 64 doubles.
+ */
 __device__ __forceinline__ double2 cta_tree2(double x, double y, double* sh)
 {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int nw = blockDim.x >> 5;
+    double v;
+    {
+        const double xa = __shfl_sync(full, x, (2 * lane) & 31), xb = __shfl_sync(full, x, (2 * lane + 1) & 31);
+        const double ya = __shfl_sync(full, y, (2 * lane) & 31), yb = __shfl_sync(full, y, (2 * lane + 1) & 31);
+        v = add_nospec(lane < 16 ? xa : ya, lane < 16 ? xb : yb);
+    }
 #pragma unroll
-    for (int m = 1; m < 32; m <<= 1) {
-        double xo = __shfl_down_sync(0xffffffffu, x, m);
-        double yo = __shfl_down_sync(0xffffffffu, y, m);
-        if ((threadIdx.x & (2 * m - 1)) == 0) {
-            x = add_nospec(x, xo);
-            y = add_nospec(y, yo);
+    for (int h = 16; h >= 2; h >>= 1) {
+        const double a = __shfl_sync(full, v, (2 * lane) & 31), b = __shfl_sync(full, v, (2 * lane + 1) & 31);
+        if (lane < h) {
+            v = add_nospec(a, b);
         }
     }
-    int nw = blockDim.x >> 5;
-    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    /* lane 0: the warp's x sum, lane 1: its y sum */
     __syncthreads();
-    if (lane == 0) {
-        sh[wid] = x;
-        sh[32 + wid] = y;
+    if (lane < 2) {
+        sh[32 * lane + wid] = v;
     }
     __syncthreads();
     if (wid == 0) {
-        double a = lane < nw ? sh[lane] : 0.0;
-        double b = lane < nw ? sh[32 + lane] : 0.0;
-#pragma unroll
-        for (int m = 1; m < 32; m <<= 1) {
-            double ao = __shfl_down_sync(0xffffffffu, a, m);
-            double bo = __shfl_down_sync(0xffffffffu, b, m);
-            if ((threadIdx.x & (2 * m - 1)) == 0) {
-                a = add_nospec(a, ao);
-                b = add_nospec(b, bo);
+        if (nw <= 16) {
+            double w = lane < nw ? sh[lane] : (lane < 2 * nw ? sh[32 + lane - nw] : 0.0);
+            for (int h = nw; h >= 2; h >>= 1) {
+                const double a = __shfl_sync(full, w, (2 * lane) & 31), b = __shfl_sync(full, w, (2 * lane + 1) & 31);
+                if (lane < h) {
+                    w = add_nospec(a, b);
+                }
             }
+            x = w;
+            y = __shfl_sync(full, w, 1);
         }
-        x = a;
-        y = b;
+        else {
+            double a = sh[lane], b = sh[32 + lane];
+#pragma unroll
+            for (int m = 1; m < 32; m <<= 1) {
+                const double ao = __shfl_down_sync(full, a, m), bo = __shfl_down_sync(full, b, m);
+                if ((lane & (2 * m - 1)) == 0) {
+                    a = add_nospec(a, ao);
+                    b = add_nospec(b, bo);
+                }
+            }
+            x = a;
+            y = b;
+        }
     }
     return make_double2(x, y);
 }
@@ -1071,6 +1204,46 @@ __device__ __forceinline__ double serial_tree(F get, int64_t lo, int64_t len)
         ++lvl;
     }
     return st[lvl];
+}
+
+/* serial_tree of two sums at once over len leaves (a power of two): aligned groups of 8 leaves are
+ * loaded together (8 loads in flight, not one) and summed as their canonical subtree in registers,
+ * then folded into the stack as above; the same additions in the same order. */
+template <class F>
+__device__ __forceinline__ double2 serial_tree2(F get, int64_t lo, int64_t len)
+{
+    if (len < 8) {
+        return make_double2(serial_tree([&](int64_t i) { return get(i).x; }, lo, len),
+                            serial_tree([&](int64_t i) { return get(i).y; }, lo, len));
+    }
+    double sx[40], sy[40];
+    const int64_t nb = len / 8;
+    for (int64_t b = 0; b < nb; ++b) {
+        double2 q[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            q[i] = get(lo + 8 * b + i);
+        }
+        double x = FQ_ADD(FQ_ADD(FQ_ADD(q[0].x, q[1].x), FQ_ADD(q[2].x, q[3].x)),
+                          FQ_ADD(FQ_ADD(q[4].x, q[5].x), FQ_ADD(q[6].x, q[7].x)));
+        double y = FQ_ADD(FQ_ADD(FQ_ADD(q[0].y, q[1].y), FQ_ADD(q[2].y, q[3].y)),
+                          FQ_ADD(FQ_ADD(q[4].y, q[5].y), FQ_ADD(q[6].y, q[7].y)));
+        int64_t j = b;
+        int lvl = 0;
+        while (j & 1) {
+            x = FQ_ADD(sx[lvl], x);
+            y = FQ_ADD(sy[lvl], y);
+            j >>= 1;
+            ++lvl;
+        }
+        sx[lvl] = x;
+        sy[lvl] = y;
+    }
+    int lvl = 0;
+    while ((int64_t(1) << lvl) < nb) {
+        ++lvl;
+    }
+    return make_double2(sx[lvl], sy[lvl]);
 }
 
 __host__ __device__ __forceinline__ int64_t next_pow2(int64_t n)

@@ -45,6 +45,8 @@ bool plain_runs_apply(const DevSys& s);
 /* Small Line1d / Particles systems: a whole run in one launch of one thread-block cluster. */
 static const int SMALL_MAX_CTAS = 16;   /* cluster size limit (above 8 needs the non-portable opt-in) */
 static const int SMALL_RING_MAX = 1024; /* StopList windows up to this length stay in shared memory */
+/* small systems keep a next-window buffer (N x nchunk doubles) up to this many values */
+static const int64_t NX_MAX_VALUES = (int64_t)1 << 25;
 static const int SMALL_THREADS_MAX = 256; /* particle threads per CTA (each CTA adds one control warp) */
 struct SmallGeom {
     int threads; /* per CTA, power of two in [32, 256] */
@@ -54,6 +56,8 @@ struct SmallGeom {
 };
 SmallGeom small_geometry(int64_t N, int max_ctas);
 cudaError_t launch_small_run(const DevSys& s, const SmallGeom& g, cudaStream_t st);
+/* refreshes the next-window buffers of a small system (no-op when it has none) */
+cudaError_t launch_next_window(const DevSys& s, cudaStream_t st);
 /* Whether a cluster of g.ctas CTAs of this kernel can be co-scheduled (sizes above 8 are opt-in). */
 bool small_cluster_fits(const DevSys& s, const SmallGeom& g);
 

@@ -237,7 +237,7 @@ __device__ void finalize_step(const DevSys& s, double uf, double sf, double sff)
 }
 
 /* Whole-CTA canonical tree over partials[0..G) (zero padded to a power of two). */
-__device__ double2 tree_partials(const double2* partials, int64_t G, double* sh)
+static __device__ __noinline__ double2 tree_partials(const double2* partials, int64_t G, double* sh)
 {
     int64_t P = next_pow2(G);
     int T = blockDim.x;
@@ -252,8 +252,10 @@ __device__ double2 tree_partials(const double2* partials, int64_t G, double* sh)
     else {
         int64_t per = P / T;
         int64_t lo = (int64_t)threadIdx.x * per;
-        x = serial_tree([&](int64_t i) { return i < G ? __ldcg(partials + i).x : 0.0; }, lo, per);
-        y = serial_tree([&](int64_t i) { return i < G ? __ldcg(partials + i).y : 0.0; }, lo, per);
+        const double2 t = serial_tree2(
+            [&](int64_t i) { return i < G ? __ldcg(partials + i) : make_double2(0.0, 0.0); }, lo, per);
+        x = t.x;
+        y = t.y;
     }
     return cta_tree2(x, y, sh);
 }
@@ -466,6 +468,7 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_line(DevSys s
 {
     __shared__ StepShared sh;
     __shared__ double sh_un[256 * PPT];
+    __shared__ double sh_halo[2]; /* ring neighbours left of the tile's first particle, right of its last */
     if (!step_prologue(s, sh, true)) {
         return;
     }
@@ -533,6 +536,13 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_line(DevSys s
         for (int j = 0; j < PPT; ++j) {
             sh_un[threadIdx.x * PPT + j] = un[j];
         }
+        if (threadIdx.x < 2) {
+            /* the two neighbours outside the tile, recomputed from the old state by two lanes of one
+             * warp (one pass through the position update instead of one in each of two warps) */
+            const int64_t last = (base + (int64_t)T * PPT < N ? base + (int64_t)T * PPT : N) - 1;
+            const int64_t q = threadIdx.x == 0 ? (base == 0 ? N - 1 : base - 1) : (last + 1 == N ? 0 : last + 1);
+            sh_halo[threadIdx.x] = u_next(s, u0, v0, a0, q);
+        }
         __syncthreads();
     }
     double rf = 0.0, rff = 0.0;
@@ -555,8 +565,8 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_line(DevSys s
         double fi = 0.0;
         if (inter_ring(INTER)) {
             int li = threadIdx.x * PPT + j;
-            double uL = li > 0 ? sh_un[li - 1] : u_next(s, u0, v0, a0, p == 0 ? N - 1 : p - 1);
-            double uR = (li + 1 < T * PPT && p + 1 < N) ? sh_un[li + 1] : u_next(s, u0, v0, a0, p + 1 == N ? 0 : p + 1);
+            double uL = li > 0 ? sh_un[li - 1] : sh_halo[0];
+            double uR = (li + 1 < T * PPT && p + 1 < N) ? sh_un[li + 1] : sh_halo[1];
             fi = ring_force<INTER, SOFT>(s, uL, up, uR);
         }
         double sfi = S_ADD(9, sfp, fi);
@@ -626,7 +636,8 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_line(DevSys s
 }
 
 /*
- * Line2d step: CTA tile of 8 rows x 32 columns, one particle per thread.  The residual terms are
+ * Line2d step: CTA tile of 8 rows x 32 columns, one particle per thread, the neighbourhood read from
+ * a haloed shared tile (the halo of 84 positions recomputed by three whole warps).  The residual terms are
  * written per particle (sq2) and summed in the flat-index pairwise order by k_reduce_grid, which
  * also finalises the step.
  */
@@ -634,7 +645,9 @@ template <int POT, int INTER = INTER_LAPLACE2D, unsigned SOFT = STEP_SOFT>
 __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_grid(DevSys s, int redo)
 {
     __shared__ StepShared sh;
-    __shared__ double sh_un[8][32];
+    /* the tile's new positions at [1 + row][1 + column], with the halo around its nr x nc valid
+     * particles: rows 0 and 1 + nr, columns 0 and 1 + nc, and the four corners */
+    __shared__ double sh_un[10][34];
     if (!step_prologue(s, sh, true)) {
         return;
     }
@@ -654,8 +667,11 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_grid(DevSys s
     const double uf = sh.uf;
     const int64_t R = s.rows, C = s.cols;
     const int tx = threadIdx.x, ty = threadIdx.y;
-    const int64_t i = (int64_t)blockIdx.y * 8 + ty;
-    const int64_t jc = (int64_t)blockIdx.x * 32 + tx;
+    const int64_t row0 = (int64_t)blockIdx.y * 8, col0 = (int64_t)blockIdx.x * 32;
+    const int nr = (int)(R - row0 < 8 ? R - row0 : 8);
+    const int nc = (int)(C - col0 < 32 ? C - col0 : 32);
+    const int64_t i = row0 + ty;
+    const int64_t jc = col0 + tx;
     const bool valid = i < R && jc < C;
     const double* u0 = s.u[cur];
     const double* v0 = s.v[cur];
@@ -666,7 +682,39 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_grid(DevSys s
         vr = v0[p];
         ar = a0[p];
         up = S_ADD(3, S_ADD(2, u0[p], S_MUL(0, s.dt, vr)), S_MUL(1, s.hdt2, ar));
-        sh_un[ty][tx] = up;
+        sh_un[1 + ty][1 + tx] = up;
+    }
+    {
+        /* the halo, recomputed from the old state (periodic) by whole warps: warp 0 the row above,
+         * warp 1 the row below, warp 2 the side columns (lanes 0-7 left, 8-15 right) and the corners
+         * (lanes 16-19) */
+        const int64_t rt = (row0 + R - 1) % R, rb = (row0 + nr) % R;
+        const int64_t cl = (col0 + C - 1) % C, cr = (col0 + nc) % C;
+        if (ty == 0 && tx < nc) {
+            sh_un[0][1 + tx] = u_next(s, u0, v0, a0, rt * C + jc);
+        }
+        else if (ty == 1 && tx < nc) {
+            sh_un[1 + nr][1 + tx] = u_next(s, u0, v0, a0, rb * C + jc);
+        }
+        else if (ty == 2 && tx < 20) {
+            int r, c;
+            int64_t q;
+            if (tx < 16) {
+                const int k = tx & 7;
+                r = 1 + k;
+                c = tx < 8 ? 0 : 1 + nc;
+                q = (row0 + k) * C + (tx < 8 ? cl : cr);
+            }
+            else {
+                const int k = tx - 16;
+                r = k < 2 ? 0 : 1 + nr;
+                c = (k & 1) ? 1 + nc : 0;
+                q = (k < 2 ? rt : rb) * C + ((k & 1) ? cr : cl);
+            }
+            if (tx >= 16 || (tx & 7) < nr) {
+                sh_un[r][c] = u_next(s, u0, v0, a0, q);
+            }
+        }
     }
     __syncthreads();
     if (valid) {
@@ -686,22 +734,15 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_grid(DevSys s
         double sfp = frame_pot<POT, SOFT>(s, w, up, uf, ff);
         double fi;
         if (INTER == INTER_LAPLACE2D) {
-            double uU = ty > 0 ? sh_un[ty - 1][tx] : u_next(s, u0, v0, a0, ((i + R - 1) % R) * C + jc);
-            double uD = (ty < 7 && i + 1 < R) ? sh_un[ty + 1][tx] : u_next(s, u0, v0, a0, ((i + 1) % R) * C + jc);
-            double uL = tx > 0 ? sh_un[ty][tx - 1] : u_next(s, u0, v0, a0, i * C + (jc + C - 1) % C);
-            double uR = (tx < 31 && jc + 1 < C) ? sh_un[ty][tx + 1] : u_next(s, u0, v0, a0, i * C + (jc + 1) % C);
+            const double uU = sh_un[ty][1 + tx];
+            const double uD = sh_un[ty + 2][1 + tx];
+            const double uL = sh_un[1 + ty][tx];
+            const double uR = sh_un[1 + ty][tx + 2];
             fi = scale(FQ_SUB(FQ_ADD(FQ_ADD(FQ_ADD(uU, uD), uL), uR), scale_pow2(up, 2, 4.0)), s.s_k);
         }
         else {
-            /* 3 x 3 neighbourhood: the tile's new positions, or recomputed from the old state outside it */
-            auto nb = [&](int di, int dj) -> double {
-                const int yy = ty + di, xx = tx + dj;
-                const int64_t ii = i + di, jj = jc + dj;
-                if (yy >= 0 && yy < 8 && xx >= 0 && xx < 32 && ii >= 0 && ii < R && jj >= 0 && jj < C) {
-                    return sh_un[yy][xx];
-                }
-                return u_next(s, u0, v0, a0, ((ii + R) % R) * C + (jj + C) % C);
-            };
+            /* 3 x 3 neighbourhood from the haloed tile */
+            auto nb = [&](int di, int dj) -> double { return sh_un[1 + ty + di][1 + tx + dj]; };
             fi = qg2d_force(s, up, nb(1, 0), nb(-1, 0), nb(0, 1), nb(0, -1), nb(1, 1), nb(1, -1), nb(-1, 1), nb(-1, -1));
         }
         double sfi = S_ADD(9, sfp, fi);
@@ -738,16 +779,18 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_grid(DevSys s
 
 /*
  * Line2d Laplace2d step with two rows per thread: CTA tile of 16 rows x 32 columns (blockDim 32 x 8,
- * thread (x, y) owns rows 2y and 2y + 1 of column x).  The vertical neighbour between a thread's two
- * particles comes from its own registers' shared-memory copy, and the recomputed halo is 96 positions
- * per 512 particles instead of 80 per 256 for 8 x 32 tiles of one particle per thread.  Per particle
- * the same operations in the same order as k_step_grid, so the same results.
+ * thread (x, y) owns rows 2y and 2y + 1 of column x).  All four neighbours come from shared memory:
+ * the tile's new positions and a recomputed halo of 96 positions per 512 particles, computed by three
+ * whole warps (the 8 x 32 tiles of k_step_grid recompute their side columns in one lane per warp and
+ * row).  Per particle the same operations in the same order as k_step_grid, so the same results.
  */
 template <int POT, unsigned SOFT = STEP_SOFT>
 __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_grid2(DevSys s, int redo)
 {
     __shared__ StepShared sh;
-    __shared__ double sh_un[16][32];
+    /* the tile's new positions at [1 + row][1 + column], with the four halo lines around them: row 0
+     * and row 1 + nr (the rows above and below the tile's nr valid rows), column 0 and column 1 + nc */
+    __shared__ double sh_un[18][34];
     if (!step_prologue(s, sh, true)) {
         return;
     }
@@ -767,8 +810,11 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_grid2(DevSys 
     const double uf = sh.uf;
     const int64_t R = s.rows, C = s.cols;
     const int tx = threadIdx.x, ty = threadIdx.y;
-    const int64_t jc = (int64_t)blockIdx.x * 32 + tx;
-    const int64_t i0 = (int64_t)blockIdx.y * 16 + 2 * ty;
+    const int64_t row0 = (int64_t)blockIdx.y * 16, col0 = (int64_t)blockIdx.x * 32;
+    const int nr = (int)(R - row0 < 16 ? R - row0 : 16);
+    const int nc = (int)(C - col0 < 32 ? C - col0 : 32);
+    const int64_t jc = col0 + tx;
+    const int64_t i0 = row0 + 2 * ty;
     const double* u0 = s.u[cur];
     const double* v0 = s.v[cur];
     const double* a0 = s.a[cur];
@@ -782,8 +828,21 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_grid2(DevSys 
             vr[q] = v0[p];
             ar[q] = a0[p];
             up[q] = S_ADD(3, S_ADD(2, u0[p], S_MUL(0, s.dt, vr[q])), S_MUL(1, s.hdt2, ar[q]));
-            sh_un[2 * ty + q][tx] = up[q];
+            sh_un[1 + 2 * ty + q][1 + tx] = up[q];
         }
+    }
+    /* the halo, recomputed from the old state (periodic): warp 0 the row above, warp 1 the row below,
+     * warp 2 the columns left (lanes 0-15) and right (lanes 16-31); whole warps, no divergent lanes */
+    if (ty == 0 && tx < nc) {
+        sh_un[0][1 + tx] = u_next(s, u0, v0, a0, ((row0 + R - 1) % R) * C + jc);
+    }
+    else if (ty == 1 && tx < nc) {
+        sh_un[1 + nr][1 + tx] = u_next(s, u0, v0, a0, ((row0 + nr) % R) * C + jc);
+    }
+    else if (ty == 2 && (tx & 15) < nr) {
+        const int r = tx & 15;
+        const int64_t c = tx < 16 ? (col0 + C - 1) % C : (col0 + nc) % C;
+        sh_un[1 + r][tx < 16 ? 0 : 1 + nc] = u_next(s, u0, v0, a0, (row0 + r) * C + c);
     }
     __syncthreads();
 #pragma unroll
@@ -808,10 +867,10 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_grid2(DevSys 
         }
         double ff;
         double sfp = frame_pot<POT, SOFT>(s, w, up[q], uf, ff);
-        double uU = r > 0 ? sh_un[r - 1][tx] : u_next(s, u0, v0, a0, ((i + R - 1) % R) * C + jc);
-        double uD = (r < 15 && i + 1 < R) ? sh_un[r + 1][tx] : u_next(s, u0, v0, a0, ((i + 1) % R) * C + jc);
-        double uL = tx > 0 ? sh_un[r][tx - 1] : u_next(s, u0, v0, a0, i * C + (jc + C - 1) % C);
-        double uR = (tx < 31 && jc + 1 < C) ? sh_un[r][tx + 1] : u_next(s, u0, v0, a0, i * C + (jc + 1) % C);
+        const double uU = sh_un[r][1 + tx];
+        const double uD = sh_un[r + 2][1 + tx];
+        const double uL = sh_un[1 + r][tx];
+        const double uR = sh_un[1 + r][tx + 2];
         double fi = scale(FQ_SUB(FQ_ADD(FQ_ADD(FQ_ADD(uU, uD), uL), uR), scale_pow2(up[q], 2, 4.0)), s.s_k);
         double sfi = S_ADD(9, sfp, fi);
         double vv, aa, f;
@@ -944,6 +1003,56 @@ __global__ void __launch_bounds__(128) k_regen(DevSys s)
         }
         __syncthreads();
     }
+}
+
+/*
+ * Next-window buffers of a small system, refreshed before a run of the one-cluster kernel: each CTA
+ * takes particles blockIdx.x, blockIdx.x + gridDim.x, ...; a particle whose buffer does not follow
+ * its current window (next_window_ready) gets the W draws after the window end from all the CTA's
+ * threads, then their running sum from one thread.  A particle whose buffer is current costs one
+ * comparison, so the kernel is cheap when few windows moved.
+ */
+__global__ void __launch_bounds__(128) k_next_window(DevSys s)
+{
+    __shared__ int need_sh, kind_sh;
+    __shared__ uint64_t st_sh;
+    __shared__ long long end_sh;
+    const uint64_t mv_c = pcg_advance(0ULL, (uint64_t)blockDim.x);
+    const uint64_t mv_a = pcg_advance(1ULL, (uint64_t)blockDim.x) - mv_c;
+    for (int64_t p = blockIdx.x; p < s.N; p += gridDim.x) {
+        if (threadIdx.x == 0) {
+            const int64_t end = s.start[p] + s.W - 1;
+            int kind;
+            int64_t ko;
+            uint64_t sto;
+            need_sh = s.nx_end[p] != end && next_window_applies(s, p, end, kind, ko, sto);
+            if (need_sh) {
+                kind_sh = kind;
+                end_sh = end;
+                st_sh = pcg_advance(sto, (uint64_t)(end + 1 - ko));
+            }
+        }
+        __syncthreads();
+        if (need_sh) {
+            seq_draws(s, s.nx + p * s.W, s.W, st_sh, (int)threadIdx.x, (int)blockDim.x, mv_a, mv_c);
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                next_window_sum(s, p, end_sh, kind_sh);
+                s.nx_end[p] = end_sh;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+cudaError_t launch_next_window(const DevSys& s, cudaStream_t st)
+{
+    if (s.nx == nullptr) {
+        return cudaSuccess;
+    }
+    const int64_t grid = s.N < 4 * 152 ? s.N : 4 * 152;
+    k_next_window<<<(unsigned)grid, 128, 0, st>>>(s);
+    return cudaGetLastError();
 }
 
 /* ------------------------------------------------------------- thermal forcing */
@@ -1693,7 +1802,9 @@ __global__ void __launch_bounds__(SMALL_THREADS_MAX + 32, 1) k_run_small(DevSys 
                     int k = atomicAdd(&sh_nmove, 1);
                     if (k < SMALL_MOVES) {
                         FwdMove m;
+                        const bool ready = next_window_ready(s, p0 + j);
                         if (fwd_move_plan(s, p0 + j, un[j], m)) {
+                            m.next = ready ? 1 : 0;
                             sh_moves[k] = m;
                             slot[j] = k;
                         }
@@ -1703,11 +1814,20 @@ __global__ void __launch_bounds__(SMALL_THREADS_MAX + 32, 1) k_run_small(DevSys 
                     }
                 }
             }
+            if (tid == 0) {
+                /* the moved windows' next-window buffers are out of date after this run */
+                atomicOr(&sc0->nx_stale, 1);
+            }
             particle_bar(pt);
             const int nm = sh_nmove < SMALL_MOVES ? sh_nmove : SMALL_MOVES;
             for (int k = 0; k < nm; ++k) {
                 if (sh_moves[k].p >= 0) {
-                    fwd_move_draws(s, sh_moves[k], tid, pt, mv_a, mv_c);
+                    if (sh_moves[k].next) {
+                        fwd_move_copy(s, sh_moves[k], tid, pt);
+                    }
+                    else {
+                        fwd_move_draws(s, sh_moves[k], tid, pt, mv_a, mv_c);
+                    }
                 }
             }
             particle_bar(pt);
@@ -1718,7 +1838,12 @@ __global__ void __launch_bounds__(SMALL_THREADS_MAX + 32, 1) k_run_small(DevSys 
                 }
                 int64_t p = p0 + j;
                 if (slot[j] >= 0) {
-                    fwd_move_sum(s, sh_moves[slot[j]]);
+                    if (sh_moves[slot[j]].next) {
+                        fwd_move_finish(s, sh_moves[slot[j]]);
+                    }
+                    else {
+                        fwd_move_sum(s, sh_moves[slot[j]]);
+                    }
                 }
                 else {
                     dev_align(s, p, un[j]); /* moves the chunk window; a failed search sets walk_flag */

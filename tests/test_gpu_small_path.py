@@ -128,3 +128,26 @@ def test_short_runs_with_window_moves(monkeypatch, kind, n):
         assert np.array_equal(small.chunk.data, graph.chunk.data), k
         moved += int(np.sum(small.chunk.start != start))
     assert moved > 0
+
+
+@pytest.mark.parametrize("n", [64, 1024])
+def test_window_moves_across_restore(monkeypatch, n):
+    """The one-cluster kernel copies the new slots of a forward window move from a next-window buffer
+    filled before the run.  chunk.restore with shifted values starts other sequences at the same
+    window positions, so the buffers must be refilled; the windows moved in the runs before and after
+    it must equal the graph path's, whose moves draw every value."""
+    small, graph = make_both(monkeypatch, "Line1d_Cuspy", n, nchunk=40, offset=-5.0, k_frame=0.5, eta=0.5)
+    for s in (small, graph):
+        s.flowSteps(800, 0.5)
+    assert_same(small, graph)
+    assert np.array_equal(small.chunk.data, graph.chunk.data)
+    start = small.chunk.start.copy()
+    assert np.max(start) > 0
+    state = small.chunk.state_at(start)
+    value = small.chunk.data[..., 0] + 0.25
+    for s in (small, graph):
+        s.chunk.restore(state=state, value=value, index=start)
+        s.flowSteps(800, 0.5)
+    assert_same(small, graph)
+    assert np.array_equal(small.chunk.data, graph.chunk.data)
+    assert np.max(small.chunk.start - start) > 0
