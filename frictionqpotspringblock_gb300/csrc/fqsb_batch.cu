@@ -325,17 +325,20 @@ __device__ void batch_iteration_end(const BatchDev& b, bool redo)
 }
 
 /*
- * One phase step of one tile: entry k of the pass's active-tile list (nact entries).  Thread t owns the
- * PPT consecutive particles t*PPT + [0, PPT) of the tile; neighbours on the realisation's ring come
- * from shared memory or are recomputed at the tile edges.
+ * One phase step of one tile.  Thread t owns the PPT consecutive particles t*PPT + [0, PPT) of the tile;
+ * neighbours on the realisation's ring come from shared memory or are recomputed at the tile edges.
  */
 template <int PPT>
-__device__ __forceinline__ void batch_tile(const BatchDev& b, int redo, int kt, int nact, BShared& sh, double* sh_un)
+__global__ void __launch_bounds__(256, 4) k_batch(BatchDev b, int redo)
 {
+    __shared__ BShared sh;
+    __shared__ double sh_un[256 * PPT];
     if (threadIdx.x == 0) {
-        /* while no realisation has finished the list is the identity (no second dependent load) */
-        sh.nact = nact;
-        sh.tile = nact == (int)b.ntiles ? kt : b.active_tiles[kt];
+        /* CTA k takes the k-th tile of an unfinished realisation; the others have nothing to do.  While
+         * no realisation has finished the list is the identity (no second dependent load). */
+        sh.nact = ((volatile BatchRun*)b.run)->n_active_tiles;
+        sh.tile = sh.nact == (int)b.ntiles ? (int)blockIdx.x
+                                            : ((int)blockIdx.x < sh.nact ? b.active_tiles[blockIdx.x] : -1);
     }
     __syncthreads();
     if (sh.tile < 0) {
@@ -660,45 +663,6 @@ __device__ __forceinline__ void batch_tile(const BatchDev& b, int redo, int kt, 
     }
 }
 
-/*
- * One pass over the active tiles: a grid of resident CTAs (batch_grid), CTA c taking list entries
- * c, c + gridDim.x, ...  Finished realisations' tiles are not in the list, so a pass costs nothing for
- * them (a grid of one CTA per tile would retire a CTA for every finished tile in every iteration).
- * The count is read once per CTA: the list changes only in the pass's last tile, after every CTA with
- * a tile of this pass has read it.
- */
-template <int PPT>
-__global__ void __launch_bounds__(256, 4) k_batch(BatchDev b, int redo)
-{
-    __shared__ BShared sh;
-    __shared__ double sh_un[256 * PPT];
-    __shared__ int nact_sh;
-    if (threadIdx.x == 0) {
-        nact_sh = ((volatile BatchRun*)b.run)->n_active_tiles;
-    }
-    __syncthreads();
-    const int nact = nact_sh;
-    for (int kt = blockIdx.x; kt < nact; kt += gridDim.x) {
-        batch_tile<PPT>(b, redo, kt, nact, sh, sh_un);
-        __syncthreads();
-    }
-}
-
-/* CTAs of a pass of k_batch: as many as the GPU holds at once, at most one per tile */
-static unsigned batch_grid(const BatchDev& b, int threads)
-{
-    const void* fk = b.ppt == 2 ? (const void*)k_batch<2> : (const void*)k_batch<1>;
-    int dev = 0, sms = 0, per_sm = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fk, threads, 0) != cudaSuccess || per_sm < 1 || sms < 1) {
-        cudaGetLastError();
-        per_sm = 1;
-        sms = 152;
-    }
-    const int64_t g = (int64_t)per_sm * sms;
-    return (unsigned)(g < b.ntiles ? g : b.ntiles);
-}
-
 /* the batch's regeneration branch: move the chunk windows recorded by pass 1 (target = new u) */
 __global__ void __launch_bounds__(128) k_batch_regen(BatchDev b)
 {
@@ -830,12 +794,11 @@ static cudaError_t build_batch_graph(BatchDev& b, int threads, cudaGraphExec_t* 
     void* a2[] = {(void*)&b, (void*)&pass2};
     void* ar[] = {(void*)&b};
     cudaGraphNode_t ns, nif, nr, nd;
-    const dim3 grid(batch_grid(b, threads));
-    BG(add_kernel_node(&ns, body, nullptr, 0, fk, grid, dim3((unsigned)threads), a1));
+    BG(add_kernel_node(&ns, body, nullptr, 0, fk, dim3((unsigned)b.ntiles), dim3((unsigned)threads), a1));
     cudaGraph_t ifb;
     BG(add_cond(&nif, body, &ns, 1, hi, cudaGraphCondTypeIf, &ifb));
     BG(add_kernel_node(&nr, ifb, nullptr, 0, (void*)k_batch_regen, dim3(4 * 152), dim3(128), ar));
-    BG(add_kernel_node(&nd, ifb, &nr, 1, fk, grid, dim3((unsigned)threads), a2));
+    BG(add_kernel_node(&nd, ifb, &nr, 1, fk, dim3((unsigned)b.ntiles), dim3((unsigned)threads), a2));
 #undef BG
     e = cudaGraphInstantiate(exec, g, 0);
     cudaGraphDestroy(g);
@@ -1254,14 +1217,13 @@ extern "C" int fqsb_batch_quasistatic(fqsb_batch* h, int64_t ncycles, double eps
         void* a1[] = {(void*)&bh, (void*)&pass1};
         void* a2[] = {(void*)&bh, (void*)&pass2};
         void* ar[] = {(void*)&bh};
-        const dim3 grid(batch_grid(b, h->threads));
         for (;;) {
-            QCU(cudaLaunchKernel(fk, grid, dim3((unsigned)h->threads), a1, 0, h->stream));
+            QCU(cudaLaunchKernel(fk, dim3((unsigned)b.ntiles), dim3((unsigned)h->threads), a1, 0, h->stream));
             QCU(cudaMemcpyAsync(&R, b.run, sizeof(R), cudaMemcpyDeviceToHost, h->stream));
             QCU(cudaStreamSynchronize(h->stream));
             if (R.n_pending_tiles > 0) {
                 QCU(cudaLaunchKernel((void*)k_batch_regen, dim3(4 * 152), dim3(128), ar, 0, h->stream));
-                QCU(cudaLaunchKernel(fk, grid, dim3((unsigned)h->threads), a2, 0, h->stream));
+                QCU(cudaLaunchKernel(fk, dim3((unsigned)b.ntiles), dim3((unsigned)h->threads), a2, 0, h->stream));
                 QCU(cudaMemcpyAsync(&R, b.run, sizeof(R), cudaMemcpyDeviceToHost, h->stream));
                 QCU(cudaStreamSynchronize(h->stream));
             }
