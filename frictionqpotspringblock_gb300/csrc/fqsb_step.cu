@@ -755,7 +755,7 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_grid(DevSys s
             sh.nan = 1;
         }
         if (resid) {
-            s.sq2[p] = make_double2(mul_nospec(f, f), mul_nospec(ff, ff));
+            s.sq2[p] = make_double2(fq_smul(f, f), fq_smul(ff, ff));
         }
     }
     if (redo) {
@@ -882,7 +882,7 @@ __global__ void __launch_bounds__(256, StepOcc<POT>::value) k_step_grid2(DevSys 
             sh.nan = 1;
         }
         if (resid) {
-            s.sq2[p] = make_double2(mul_nospec(f, f), mul_nospec(ff, ff));
+            s.sq2[p] = make_double2(fq_smul(f, f), fq_smul(ff, ff));
         }
     }
     if (redo) {
